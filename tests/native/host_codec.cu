@@ -1,0 +1,162 @@
+// host_codec.cu -- runs the GPU block codec (zfp_gb300/csrc/codec.cuh) on the
+// CPU over whole fields, block after block in raster order, so the tests can
+// compare its per-block logic with the oracle without a GPU.  Test-only; the
+// product library never contains this file.
+#include <cstddef>
+#include <cstdint>
+#include <cstring>
+
+#include "../../zfp_gb300/csrc/codec.cuh"
+
+namespace {
+
+struct VecSink {
+  uint64_t* words;
+  uint64_t pos;
+  ZG_HD void put(uint64_t v, unsigned n) {
+    if (!n) return;
+    v = zg::low_bits(v, n);
+    const unsigned o = (unsigned)(pos & 63);
+    words[pos >> 6] |= v << o;
+    if (o && o + n > 64) words[(pos >> 6) + 1] |= v >> (64 - o);
+    pos += n;
+  }
+  ZG_HD void pad(unsigned n) { pos += n; }
+};
+
+struct Geom {
+  int dims;
+  size_t n[4], nb[4];
+  ptrdiff_t s[4];
+  size_t blocks;
+};
+
+Geom geom(int dims, const size_t* n, const ptrdiff_t* s) {
+  Geom g;
+  g.dims = dims;
+  g.blocks = 1;
+  for (int a = 0; a < 4; a++) {
+    g.n[a] = a < dims ? n[a] : 1;
+    g.nb[a] = (g.n[a] + 3) / 4;
+    g.blocks *= g.nb[a];
+  }
+  g.s[0] = s[0] ? s[0] : 1;
+  g.s[1] = s[1] ? s[1] : (ptrdiff_t)n[0];
+  g.s[2] = s[2] ? s[2] : (ptrdiff_t)(n[0] * g.n[1]);
+  g.s[3] = s[3] ? s[3] : (ptrdiff_t)(n[0] * g.n[1] * g.n[2]);
+  return g;
+}
+
+int pad_index(int i, size_t cnt) { return i < (int)cnt ? i : (cnt == 2 && i == 2) ? 1 : 0; }
+
+template <typename B, int D>
+void gather(const Geom& g, const B* data, size_t b, B (&raw)[1 << (2 * D)], size_t org[4], size_t cnt[4]) {
+  for (int a = 0; a < 4; a++) {
+    size_t i = b % g.nb[a];
+    b /= g.nb[a];
+    org[a] = 4 * i;
+    cnt[a] = g.n[a] - org[a] < 4 ? g.n[a] - org[a] : 4;
+  }
+  const int e[4] = {D >= 1 ? 4 : 1, D >= 2 ? 4 : 1, D >= 3 ? 4 : 1, D >= 4 ? 4 : 1};
+  int i = 0;
+  for (int w = 0; w < e[3]; w++)
+    for (int z = 0; z < e[2]; z++)
+      for (int y = 0; y < e[1]; y++)
+        for (int x = 0; x < e[0]; x++, i++) {
+          ptrdiff_t off = (ptrdiff_t)(org[0] + pad_index(x, cnt[0])) * g.s[0] +
+                          (ptrdiff_t)(org[1] + pad_index(y, cnt[1])) * g.s[1] +
+                          (ptrdiff_t)(org[2] + pad_index(z, cnt[2])) * g.s[2] +
+                          (ptrdiff_t)(org[3] + pad_index(w, cnt[3])) * g.s[3];
+          raw[i] = data[off];
+        }
+}
+
+template <typename S, int D>
+uint64_t compress_t(const Geom& g, const zg::BlockParams& p, const void* data, uint64_t* words, uint64_t bit0) {
+  using B = typename zg::Traits<S>::Bits;
+  VecSink out{words, bit0};
+  for (size_t b = 0; b < g.blocks; b++) {
+    B raw[1 << (2 * D)];
+    size_t org[4], cnt[4];
+    gather<B, D>(g, (const B*)data, b, raw, org, cnt);
+    zg::encode_block<S, D>(out, p, raw);
+  }
+  return out.pos;
+}
+
+template <typename S, int D>
+uint64_t decompress_t(const Geom& g, const zg::BlockParams& p, void* data, const uint64_t* words,
+                      uint64_t cap, uint64_t bit0) {
+  using B = typename zg::Traits<S>::Bits;
+  zg::WordSource in;
+  in.base = words;
+  in.cap = cap;
+  in.seek(bit0);
+  for (size_t b = 0; b < g.blocks; b++) {
+    B raw[1 << (2 * D)];
+    zg::decode_block<S, D>(in, p, raw);
+    size_t org[4], cnt[4];
+    size_t bb = b;
+    for (int a = 0; a < 4; a++) {
+      size_t i = bb % g.nb[a];
+      bb /= g.nb[a];
+      org[a] = 4 * i;
+      cnt[a] = g.n[a] - org[a] < 4 ? g.n[a] - org[a] : 4;
+    }
+    for (size_t w = 0; w < cnt[3]; w++)
+      for (size_t z = 0; z < cnt[2]; z++)
+        for (size_t y = 0; y < cnt[1]; y++)
+          for (size_t x = 0; x < cnt[0]; x++) {
+            ptrdiff_t off = (ptrdiff_t)(org[0] + x) * g.s[0] + (ptrdiff_t)(org[1] + y) * g.s[1] +
+                            (ptrdiff_t)(org[2] + z) * g.s[2] + (ptrdiff_t)(org[3] + w) * g.s[3];
+            ((B*)data)[off] = raw[x + 4 * y + 16 * z + 64 * w];
+          }
+  }
+  return in.at;
+}
+
+template <typename S>
+uint64_t compress_s(const Geom& g, const zg::BlockParams& p, const void* d, uint64_t* w, uint64_t b0) {
+  switch (g.dims) {
+    case 1: return compress_t<S, 1>(g, p, d, w, b0);
+    case 2: return compress_t<S, 2>(g, p, d, w, b0);
+    case 3: return compress_t<S, 3>(g, p, d, w, b0);
+    default: return compress_t<S, 4>(g, p, d, w, b0);
+  }
+}
+
+template <typename S>
+uint64_t decompress_s(const Geom& g, const zg::BlockParams& p, void* d, const uint64_t* w, uint64_t cap, uint64_t b0) {
+  switch (g.dims) {
+    case 1: return decompress_t<S, 1>(g, p, d, w, cap, b0);
+    case 2: return decompress_t<S, 2>(g, p, d, w, cap, b0);
+    case 3: return decompress_t<S, 3>(g, p, d, w, cap, b0);
+    default: return decompress_t<S, 4>(g, p, d, w, cap, b0);
+  }
+}
+
+}  // namespace
+
+extern "C" uint64_t zgh_compress(int type, int dims, const size_t* n, const ptrdiff_t* s,
+                                 const void* data, const unsigned* prm, uint64_t* words, uint64_t bit0) {
+  Geom g = geom(dims, n, s);
+  zg::BlockParams p{prm[0], prm[1], prm[2], (int32_t)prm[3]};
+  switch (type) {
+    case 1: return compress_s<int32_t>(g, p, data, words, bit0);
+    case 2: return compress_s<int64_t>(g, p, data, words, bit0);
+    case 3: return compress_s<float>(g, p, data, words, bit0);
+    default: return compress_s<double>(g, p, data, words, bit0);
+  }
+}
+
+extern "C" uint64_t zgh_decompress(int type, int dims, const size_t* n, const ptrdiff_t* s, void* data,
+                                   const unsigned* prm, const uint64_t* words, uint64_t cap, uint64_t bit0) {
+  Geom g = geom(dims, n, s);
+  zg::BlockParams p{prm[0], prm[1], prm[2], (int32_t)prm[3]};
+  switch (type) {
+    case 1: return decompress_s<int32_t>(g, p, data, words, cap, bit0);
+    case 2: return decompress_s<int64_t>(g, p, data, words, cap, bit0);
+    case 3: return decompress_s<float>(g, p, data, words, cap, bit0);
+    default: return decompress_s<double>(g, p, data, words, cap, bit0);
+  }
+}

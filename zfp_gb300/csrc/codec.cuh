@@ -1,0 +1,970 @@
+// codec.cuh -- zfp fixed-/variable-rate block codec, one zfp block per thread.
+//
+// Everything here is __host__ __device__ so the per-block logic can be run on
+// the CPU against the oracle; the kernels (encode.cu / decode.cu) supply the
+// bit sinks/sources, gather/scatter and the stream assembly.
+//
+// Design (GB300-first, not a translation of src/cuda_zfp):
+//  * a thread owns one 4^d block; for d <= 3 the whole block lives in
+//    registers (all loops unrolled, coefficient permutation resolved at
+//    compile time);
+//  * bit planes are formed by a register bit-matrix transpose (byte-permute
+//    for the 16/8-bit levels, masked swaps below) instead of per-bit loops;
+//  * group tests are coded one significance event at a time with
+//    count-trailing-zeros, never bit by bit;
+//  * the rate-limited and whole-plane coders of the reference are one coder
+//    here: the rate-limited stream is the whole-plane stream cut at maxbits
+//    (src/template/encode.c:92-256), which is exactly what a per-bit budget
+//    produces.
+// Bit-level format: src/template/encodef.c:63-90 (lossy floating point),
+// encode.c:260-280 (integers), revencode*.c (reversible),
+// include/zfp/bitstream.inl:226-313 (64-bit words, LSB first).
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+#include <type_traits>
+
+#if defined(__CUDACC__)
+#define ZG_HD __host__ __device__ __forceinline__
+#else
+#define ZG_HD inline
+#endif
+
+namespace zg {
+
+// ---------------------------------------------------------------------------
+// scalar traits (src/traits{f,d,i,l}.h)
+
+template <typename S> struct Traits;
+template <> struct Traits<float> {
+  using Bits = uint32_t; using Int = int32_t; using UInt = uint32_t;
+  static constexpr bool kFloat = true;
+  static constexpr int kPrec = 32, kEBits = 8, kEBias = 127, kPBits = 5, kMant = 23;
+};
+template <> struct Traits<double> {
+  using Bits = uint64_t; using Int = int64_t; using UInt = uint64_t;
+  static constexpr bool kFloat = true;
+  static constexpr int kPrec = 64, kEBits = 11, kEBias = 1023, kPBits = 6, kMant = 52;
+};
+template <> struct Traits<int32_t> {
+  using Bits = uint32_t; using Int = int32_t; using UInt = uint32_t;
+  static constexpr bool kFloat = false;
+  static constexpr int kPrec = 32, kEBits = 0, kEBias = 0, kPBits = 5, kMant = 0;
+};
+template <> struct Traits<int64_t> {
+  using Bits = uint64_t; using Int = int64_t; using UInt = uint64_t;
+  static constexpr bool kFloat = false;
+  static constexpr int kPrec = 64, kEBits = 0, kEBias = 0, kPBits = 6, kMant = 0;
+};
+
+constexpr int kMinExp = -1074;  // ZFP_MIN_EXP; minexp below it selects reversible mode
+
+struct BlockParams {
+  uint32_t minbits, maxbits, maxprec;
+  int32_t minexp;
+};
+
+// ---------------------------------------------------------------------------
+// bit helpers with host equivalents
+
+ZG_HD unsigned ctz64(uint64_t x) {
+#if defined(__CUDA_ARCH__)
+  return (unsigned)(__ffsll((long long)x) - 1);
+#else
+  return (unsigned)__builtin_ctzll(x);
+#endif
+}
+
+ZG_HD uint32_t byte_perm(uint32_t x, uint32_t y, uint32_t s) {
+#if defined(__CUDA_ARCH__)
+  return __byte_perm(x, y, s);
+#else
+  uint64_t xy = ((uint64_t)y << 32) | x;
+  uint32_t r = 0;
+  for (int i = 0; i < 4; i++)
+    r |= (uint32_t)((xy >> (8 * ((s >> (4 * i)) & 7))) & 0xff) << (8 * i);
+  return r;
+#endif
+}
+
+ZG_HD uint64_t low_bits(uint64_t v, unsigned n) { return n >= 64 ? v : v & ((uint64_t(1) << n) - 1); }
+
+// ---------------------------------------------------------------------------
+// coefficient order (src/template/codec{2,3,4}.c): by total sequency
+// i+j+k(+l), then by i^2+j^2+k^2(+l^2); ties in the order the format fixes.
+// Index = i + 4j + 16k + 64l.  The tables are packed at compile time into
+// 64-bit constants so that, in unrolled code, perm<D>(i) folds to a
+// register index.
+
+namespace detail {
+constexpr unsigned char kOrder2[16] = {0, 1, 4, 5, 2, 8, 6, 9, 3, 12, 10, 7, 13, 11, 14, 15};
+constexpr unsigned char kOrder3[64] = {
+    0, 1, 4, 16, 20, 17, 5, 2, 8, 32, 21, 6, 18, 24, 9, 33,
+    36, 3, 12, 48, 22, 25, 37, 40, 34, 10, 7, 19, 28, 13, 49, 52,
+    41, 38, 26, 23, 29, 53, 11, 35, 44, 14, 50, 56, 42, 27, 39, 45,
+    30, 54, 57, 60, 51, 15, 43, 46, 58, 61, 55, 31, 62, 59, 47, 63};
+constexpr uint64_t pack2() {
+  uint64_t v = 0;
+  for (int i = 0; i < 16; i++) v |= (uint64_t)kOrder2[i] << (4 * i);
+  return v;
+}
+constexpr uint64_t pack3(int w) {
+  uint64_t v = 0;
+  for (int j = 0; j < 10 && 10 * w + j < 64; j++) v |= (uint64_t)kOrder3[10 * w + j] << (6 * j);
+  return v;
+}
+constexpr uint64_t kP2 = pack2();
+constexpr uint64_t kP3_0 = pack3(0), kP3_1 = pack3(1), kP3_2 = pack3(2), kP3_3 = pack3(3),
+                   kP3_4 = pack3(4), kP3_5 = pack3(5), kP3_6 = pack3(6);
+}  // namespace detail
+
+// 4D order is only read by the rolled 4D path (runtime index); one copy per
+// translation unit since the library is built without relocatable device code
+#define ZG_ORDER4_DATA \
+    0, 1, 4, 16, 64, 5, 80, 17, 68, 65, 20, 2, 8, 32, 128, 84, \
+    81, 69, 21, 6, 18, 66, 24, 72, 9, 96, 33, 36, 129, 132, 144, 3, \
+    12, 48, 192, 85, 82, 70, 22, 73, 25, 88, 37, 100, 97, 148, 145, 133, \
+    10, 160, 34, 136, 130, 40, 7, 19, 67, 28, 76, 13, 112, 49, 52, 193, \
+    196, 208, 86, 89, 101, 149, 161, 137, 41, 134, 38, 164, 26, 152, 146, 104, \
+    98, 74, 83, 71, 23, 77, 29, 92, 53, 116, 113, 212, 209, 197, 11, 35, \
+    131, 44, 140, 14, 176, 50, 56, 194, 200, 224, 90, 165, 102, 153, 150, 105, \
+    168, 162, 138, 42, 87, 93, 117, 213, 27, 75, 99, 39, 135, 147, 108, 45, \
+    141, 156, 30, 78, 177, 180, 54, 114, 120, 57, 198, 210, 216, 201, 225, 228, \
+    15, 240, 51, 204, 195, 60, 169, 166, 154, 106, 91, 103, 151, 109, 157, 94, \
+    181, 118, 121, 214, 217, 229, 163, 139, 43, 142, 46, 172, 58, 184, 178, 232, \
+    226, 202, 241, 205, 61, 199, 55, 244, 31, 220, 211, 124, 115, 79, 170, 167, \
+    155, 107, 158, 110, 173, 122, 185, 182, 233, 230, 218, 95, 245, 119, 221, 215, \
+    125, 242, 206, 62, 203, 59, 248, 47, 236, 227, 188, 179, 143, 171, 174, 186, \
+    234, 246, 222, 126, 219, 123, 249, 111, 237, 231, 189, 183, 159, 252, 243, 207, \
+    63, 175, 250, 187, 238, 235, 190, 253, 247, 223, 127, 254, 251, 239, 191, 255,
+#if defined(__CUDACC__)
+static __device__ __constant__ unsigned char kOrder4Dev[256] = {ZG_ORDER4_DATA};
+#endif
+static const unsigned char kOrder4Host[256] = {ZG_ORDER4_DATA};
+#undef ZG_ORDER4_DATA
+
+template <int D>
+ZG_HD int perm(int i) {
+  if (D == 1) return i;
+  if (D == 2) return (int)((detail::kP2 >> (4 * i)) & 15);
+  if (D == 3) {
+    const uint64_t w = i < 10 ? detail::kP3_0 : i < 20 ? detail::kP3_1 : i < 30 ? detail::kP3_2
+                     : i < 40 ? detail::kP3_3 : i < 50 ? detail::kP3_4 : i < 60 ? detail::kP3_5
+                     : detail::kP3_6;
+    return (int)((w >> (6 * (i % 10))) & 63);
+  }
+#if defined(__CUDA_ARCH__)
+  return kOrder4Dev[i];
+#else
+  return kOrder4Host[i];
+#endif
+}
+
+// ---------------------------------------------------------------------------
+// IEEE-754 helpers (replace libm frexp/ldexp with exact bit arithmetic)
+
+template <typename S> ZG_HD S from_bits(typename Traits<S>::Bits b) {
+#if defined(__CUDA_ARCH__)
+  if constexpr (sizeof(S) == 4) return __int_as_float((int)b);
+  else return __longlong_as_double((long long)b);
+#else
+  S s; std::memcpy(&s, &b, sizeof s); return s;
+#endif
+}
+template <typename S> ZG_HD typename Traits<S>::Bits to_bits(S s) {
+#if defined(__CUDA_ARCH__)
+  if constexpr (sizeof(S) == 4) return (uint32_t)__float_as_int(s);
+  else return (uint64_t)__double_as_longlong(s);
+#else
+  typename Traits<S>::Bits b; std::memcpy(&b, &s, sizeof b); return b;
+#endif
+}
+
+// 2^e rounded like ldexp(1, e): inf above range, exact subnormals, 0 below
+// half of the smallest subnormal
+template <typename S> ZG_HD S pow2(int e) {
+  using T = Traits<S>;
+  using B = typename T::Bits;
+  constexpr int kEminSub = 1 - T::kEBias - T::kMant;
+  B b;
+  if (e > T::kEBias) b = B((B(1) << T::kEBits) - 1) << T::kMant;
+  else if (e >= 1 - T::kEBias) b = B(e + T::kEBias) << T::kMant;
+  else if (e >= kEminSub) b = B(1) << (e - kEminSub);
+  else b = 0;
+  return from_bits<S>(b);
+}
+
+template <typename S> ZG_HD S fmul(S a, S b) {
+#if defined(__CUDA_ARCH__)
+  if constexpr (sizeof(S) == 4) return __fmul_rn(a, b);
+  else return __dmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+
+// truncating float -> integer of the same width; valid for |x| < 2^(p-1)
+template <typename S> ZG_HD typename Traits<S>::Int trunc_int(S x) {
+#if defined(__CUDA_ARCH__)
+  if constexpr (sizeof(S) == 4) return __float2int_rz(x);
+  else return __double2ll_rz(x);
+#else
+  return (typename Traits<S>::Int)x;
+#endif
+}
+
+// round-to-nearest integer -> float of the same width
+template <typename S> ZG_HD S int_to_float(typename Traits<S>::Int i) {
+#if defined(__CUDA_ARCH__)
+  if constexpr (sizeof(S) == 4) return __int2float_rn(i);
+  else return __ll2double_rn(i);
+#else
+  return (S)i;
+#endif
+}
+
+// number of bit planes to code (src/template/codecf.c:6-13)
+ZG_HD unsigned coded_precision(int emax, unsigned maxprec, int minexp, int dims) {
+  long long p = (long long)emax - minexp + 2 * dims + 2;
+  if (p < 0) p = 0;
+  return (unsigned long long)p < maxprec ? (unsigned)p : maxprec;
+}
+
+// Largest normalised exponent of the block's finite/infinite |values|
+// (src/template/encodef.c:11-40).  NaNs never win the reference's
+// `max < f` test; an infinite maximum gets exponent 0 (glibc frexp).
+// `special` reports a NaN or infinity anywhere in the block.
+template <typename S, int N>
+ZG_HD int block_emax(const typename Traits<S>::Bits (&raw)[N], bool& special) {
+  using T = Traits<S>;
+  using B = typename T::Bits;
+  constexpr B kAbs = ~(B(1) << (8 * sizeof(B) - 1));
+  constexpr B kInf = B((B(1) << T::kEBits) - 1) << T::kMant;
+  B top = 0;
+#pragma unroll (N <= 64 ? N : 1)
+  for (int i = 0; i < N; i++) {
+    B a = raw[i] & kAbs;
+    top = a > top ? a : top;
+  }
+  special = top >= kInf;
+  if (special) {
+    top = 0;
+    for (int i = 0; i < N; i++) {
+      B a = raw[i] & kAbs;
+      if (a <= kInf && a > top) top = a;
+    }
+  }
+  if (top == 0) return -T::kEBias;
+  if (top == kInf) return 0;
+  int biased = (int)(top >> T::kMant);
+  return biased ? biased - (T::kEBias - 1) : 1 - T::kEBias;
+}
+
+// block-floating-point cast (src/template/encodef.c:44-59).  Out-of-range
+// or NaN products give the x86 integer-indefinite value, as the reference
+// does on x86-64; that only happens in blocks with NaN/inf or with a scale
+// factor that overflows (tiny blocks), so the common path has no checks.
+template <typename S, int N>
+ZG_HD void fwd_cast(const typename Traits<S>::Bits (&raw)[N], typename Traits<S>::Int (&v)[N],
+                    int emax, bool special) {
+  using T = Traits<S>;
+  using I = typename T::Int;
+  const int se = T::kPrec - 2 - emax;
+  const S s = pow2<S>(se);
+  if (!special && se <= T::kEBias) {
+#pragma unroll (N <= 64 ? N : 1)
+    for (int i = 0; i < N; i++) v[i] = trunc_int<S>(fmul<S>(s, from_bits<S>(raw[i])));
+  } else {
+    const S lim = pow2<S>(T::kPrec - 1);
+    for (int i = 0; i < N; i++) {
+      S x = fmul<S>(s, from_bits<S>(raw[i]));
+      v[i] = (x < lim && x > -lim) ? trunc_int<S>(x) : (I)((typename T::UInt)1 << (T::kPrec - 1));
+    }
+  }
+}
+
+// inverse cast (src/template/codecf.c:17-32)
+template <typename S, int N>
+ZG_HD void inv_cast(const typename Traits<S>::Int (&v)[N], typename Traits<S>::Bits (&raw)[N], int emax) {
+  using T = Traits<S>;
+  const S s = pow2<S>(emax - (T::kPrec - 2));
+#pragma unroll (N <= 64 ? N : 1)
+  for (int i = 0; i < N; i++) raw[i] = to_bits<S>(fmul<S>(s, int_to_float<S>(v[i])));
+}
+
+// ---------------------------------------------------------------------------
+// lifting steps (src/template/encode.c:31-56, decode.c:9-45,
+// revencode.c:7-33, revdecode.c:7-33); integers wrap like the reference
+
+template <typename I>
+ZG_HD void fwd_lift(I& a, I& b, I& c, I& d) {
+  using U = typename std::make_unsigned<I>::type;
+  a = (I)((U)a + (U)d); a >>= 1; d = (I)((U)d - (U)a);
+  c = (I)((U)c + (U)b); c >>= 1; b = (I)((U)b - (U)c);
+  a = (I)((U)a + (U)c); a >>= 1; c = (I)((U)c - (U)a);
+  d = (I)((U)d + (U)b); d >>= 1; b = (I)((U)b - (U)d);
+  d = (I)((U)d + (U)(b >> 1)); b = (I)((U)b - (U)(d >> 1));
+}
+
+template <typename I>
+ZG_HD void inv_lift(I& a, I& b, I& c, I& d) {
+  using U = typename std::make_unsigned<I>::type;
+  b = (I)((U)b + (U)(d >> 1)); d = (I)((U)d - (U)(b >> 1));
+  b = (I)((U)b + (U)d); d = (I)((U)d - ((U)b - (U)d));
+  c = (I)((U)c + (U)a); a = (I)((U)a - ((U)c - (U)a));
+  b = (I)((U)b + (U)c); c = (I)((U)c - ((U)b - (U)c));
+  d = (I)((U)d + (U)a); a = (I)((U)a - ((U)d - (U)a));
+}
+
+template <typename I>
+ZG_HD void rev_fwd_lift(I& a, I& b, I& c, I& d) {
+  using U = typename std::make_unsigned<I>::type;
+  U x = (U)a, y = (U)b, z = (U)c, w = (U)d;
+  w -= z; z -= y; y -= x;
+  w -= z; z -= y;
+  w -= z;
+  a = (I)x; b = (I)y; c = (I)z; d = (I)w;
+}
+
+template <typename I>
+ZG_HD void rev_inv_lift(I& a, I& b, I& c, I& d) {
+  using U = typename std::make_unsigned<I>::type;
+  U x = (U)a, y = (U)b, z = (U)c, w = (U)d;
+  w += z;
+  z += y; w += z;
+  y += x; z += y; w += z;
+  a = (I)x; b = (I)y; c = (I)z; d = (I)w;
+}
+
+// Separable transform over a 4^D block: axes x, y, z, w in that order for
+// the forward direction, the reverse order for the inverse
+// (src/template/encode3.c:35-50, decode3.c:27-42, encode4.c:42-65).
+enum LiftKind { kFwd, kInv, kRevFwd, kRevInv };
+
+template <LiftKind K, typename I>
+ZG_HD void lift(I& a, I& b, I& c, I& d) {
+  if constexpr (K == kFwd) fwd_lift(a, b, c, d);
+  else if constexpr (K == kInv) inv_lift(a, b, c, d);
+  else if constexpr (K == kRevFwd) rev_fwd_lift(a, b, c, d);
+  else rev_inv_lift(a, b, c, d);
+}
+
+template <LiftKind K, int D, typename I>
+ZG_HD void xform(I (&v)[1 << (2 * D)]) {
+  constexpr int N = 1 << (2 * D);
+  constexpr bool kInverse = (K == kInv || K == kRevInv);
+#pragma unroll
+  for (int step = 0; step < D; step++) {
+    const int axis = kInverse ? D - 1 - step : step;
+    const int s = 1 << (2 * axis);
+#pragma unroll (N <= 64 ? N : 1)
+    for (int i = 0; i < N; i++)
+      if (((i >> (2 * axis)) & 3) == 0) lift<K>(v[i], v[i + s], v[i + 2 * s], v[i + 3 * s]);
+  }
+}
+
+// negabinary (src/template/encode.c:76-79, decode.c:64-67)
+template <typename U> ZG_HD U nb_mask() { return (U)0xaaaaaaaaaaaaaaaaull; }
+template <typename I> ZG_HD typename std::make_unsigned<I>::type to_nb(I x) {
+  using U = typename std::make_unsigned<I>::type;
+  return ((U)x + nb_mask<U>()) ^ nb_mask<U>();
+}
+template <typename I> ZG_HD I from_nb(typename std::make_unsigned<I>::type u) {
+  using U = typename std::make_unsigned<I>::type;
+  return (I)((u ^ nb_mask<U>()) - nb_mask<U>());
+}
+
+// ---------------------------------------------------------------------------
+// bit planes: P[k] bit i = bit k of coefficient i (coefficients in coding
+// order).  32x32 bit-matrix transpose: byte permutes for the 16- and 8-bit
+// levels, masked swaps for 4, 2, 1.  It is its own inverse.
+
+ZG_HD void transpose32(uint32_t (&a)[32]) {
+#pragma unroll
+  for (int i = 0; i < 16; i++) {
+    uint32_t x = a[i], y = a[i + 16];
+    a[i] = byte_perm(x, y, 0x5410);
+    a[i + 16] = byte_perm(x, y, 0x7632);
+  }
+#pragma unroll
+  for (int i = 0; i < 32; i++)
+    if ((i & 8) == 0) {
+      uint32_t x = a[i], y = a[i + 8];
+      a[i] = byte_perm(x, y, 0x6240);
+      a[i + 8] = byte_perm(x, y, 0x7351);
+    }
+#pragma unroll
+  for (int i = 0; i < 32; i++)
+    if ((i & 4) == 0) {
+      uint32_t t = ((a[i] >> 4) ^ a[i + 4]) & 0x0f0f0f0fu;
+      a[i] ^= t << 4; a[i + 4] ^= t;
+    }
+#pragma unroll
+  for (int i = 0; i < 32; i++)
+    if ((i & 2) == 0) {
+      uint32_t t = ((a[i] >> 2) ^ a[i + 2]) & 0x33333333u;
+      a[i] ^= t << 2; a[i + 2] ^= t;
+    }
+#pragma unroll
+  for (int i = 0; i < 32; i++)
+    if ((i & 1) == 0) {
+      uint32_t t = ((a[i] >> 1) ^ a[i + 1]) & 0x55555555u;
+      a[i] ^= t << 1; a[i + 1] ^= t;
+    }
+}
+
+// coefficients (N <= 64) -> planes
+template <int N, typename U, int P>
+ZG_HD void make_planes(const U (&u)[N], uint64_t (&pl)[P]) {
+  static_assert(N <= 64, "wide blocks use the rolled coder");
+  if constexpr (N == 4) {
+#pragma unroll
+    for (int k = 0; k < P; k++) {
+      uint64_t x = 0;
+#pragma unroll
+      for (int i = 0; i < 4; i++) x |= (uint64_t)((u[i] >> k) & 1u) << i;
+      pl[k] = x;
+    }
+  } else {
+    uint32_t a[32];
+#pragma unroll
+    for (int half = 0; half < (int)sizeof(U) / 4; half++) {      // which 32-bit half of U
+#pragma unroll
+      for (int grp = 0; grp < (N + 31) / 32; grp++) {            // coefficients 0..31 / 32..63
+#pragma unroll
+        for (int i = 0; i < 32; i++) {
+          const int c = 32 * grp + i;
+          a[i] = c < N ? (uint32_t)((uint64_t)u[c < N ? c : 0] >> (32 * half)) : 0u;
+        }
+        transpose32(a);
+#pragma unroll
+        for (int k = 0; k < 32; k++) {
+          if (grp == 0) pl[32 * half + k] = a[k];
+          else pl[32 * half + k] |= (uint64_t)a[k] << 32;
+        }
+      }
+    }
+  }
+}
+
+// planes -> coefficients
+template <int N, typename U, int P>
+ZG_HD void take_planes(const uint64_t (&pl)[P], U (&u)[N]) {
+  static_assert(N <= 64, "wide blocks use the rolled coder");
+  if constexpr (N == 4) {
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      U x = 0;
+#pragma unroll
+      for (int k = 0; k < P; k++) x |= (U)((pl[k] >> i) & 1u) << k;
+      u[i] = x;
+    }
+  } else {
+    uint32_t a[32];
+#pragma unroll
+    for (int i = 0; i < N; i++) u[i] = 0;
+#pragma unroll
+    for (int half = 0; half < (int)sizeof(U) / 4; half++) {
+#pragma unroll
+      for (int grp = 0; grp < (N + 31) / 32; grp++) {
+#pragma unroll
+        for (int k = 0; k < 32; k++) a[k] = (uint32_t)(pl[32 * half + k] >> (32 * grp));
+        transpose32(a);
+#pragma unroll
+        for (int i = 0; i < 32; i++) {
+          const int c = 32 * grp + i;
+          if (c < N) u[c < N ? c : 0] |= (U)((uint64_t)a[i] << (32 * half));
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// embedded coder for N <= 64 coefficients (one 64-bit word per plane).
+// Every output bit costs one unit of budget; see the header comment.
+
+template <int P, int N, class Sink>
+ZG_HD unsigned encode_planes(Sink& out, unsigned budget, unsigned maxprec, const uint64_t (&pl)[P]) {
+  const int kmin = (unsigned)P > maxprec ? P - (int)maxprec : 0;
+  unsigned bits = budget, n = 0;
+#pragma unroll
+  for (int k = P - 1; k >= 0; k--) {
+    if (k < kmin || !bits) break;
+    const uint64_t x = pl[k];
+    const unsigned m = n < bits ? n : bits;
+    out.put(x, m);
+    bits -= m;
+    if (n < (unsigned)N && bits) {
+      uint64_t r = x >> n;
+      while (bits) {
+        bits--;
+        if (!r) { out.put(0, 1); break; }        // negative group test: plane done
+        out.put(1, 1);                            // positive group test
+        const unsigned z = ctz64(r);              // zeros before the next one
+        if (n + z == (unsigned)N - 1) {           // last coefficient: its one is implied
+          const unsigned e = z < bits ? z : bits;
+          out.put(0, e);
+          bits -= e;
+          n = N;
+          break;
+        }
+        const unsigned len = z + 1, e = len < bits ? len : bits;
+        out.put(uint64_t(1) << z, e);
+        bits -= e;
+        if (e < len) break;
+        n += len;
+        r >>= len;
+      }
+    }
+  }
+  return budget - bits;
+}
+
+// Decoder twin (src/template/decode.c:80-278).  When the budget ends inside
+// a positive group test the reference still deposits a one at the scan
+// position; so does this.
+template <int P, int N, class Source>
+ZG_HD unsigned decode_planes(Source& in, unsigned budget, unsigned maxprec, uint64_t (&pl)[P]) {
+  const int kmin = (unsigned)P > maxprec ? P - (int)maxprec : 0;
+  unsigned bits = budget, n = 0;
+#pragma unroll
+  for (int k = P - 1; k >= 0; k--) {
+    uint64_t x = 0;
+    if (k >= kmin && bits) {
+      const unsigned m = n < bits ? n : bits;
+      x = in.read(m);
+      bits -= m;
+      while (bits && n < (unsigned)N) {
+        bits--;
+        if (!in.read(1)) break;
+        unsigned avail = N - 1 - n;
+        if (avail > bits) avail = bits;
+        const uint64_t w = in.peek(avail);
+        unsigned z;
+        if (w) { z = ctz64(w); in.skip(z + 1); bits -= z + 1; }
+        else { z = avail; in.skip(avail); bits -= avail; }
+        n += z;
+        x |= uint64_t(1) << n;
+        n++;
+      }
+    }
+    pl[k] = x;
+  }
+  return budget - bits;
+}
+
+// Rolled coder for 4D blocks (256 coefficients), planes formed on the fly.
+template <typename U, class Sink>
+ZG_HD unsigned encode_planes_wide(Sink& out, unsigned budget, unsigned maxprec, const U (&u)[256]) {
+  constexpr int P = 8 * sizeof(U), N = 256;
+  const int kmin = (unsigned)P > maxprec ? P - (int)maxprec : 0;
+  unsigned bits = budget, n = 0;
+  for (int k = P - 1; k >= kmin && bits; k--) {
+    uint64_t pl[4] = {0, 0, 0, 0};
+    for (int i = 0; i < N; i++) pl[i >> 6] |= (uint64_t)((u[i] >> k) & 1u) << (i & 63);
+    const unsigned m = n < bits ? n : bits;
+    for (unsigned i = 0; i < m; i += 64) out.put(pl[i >> 6], m - i < 64 ? m - i : 64);
+    bits -= m;
+    while (bits && n < (unsigned)N) {
+      bits--;
+      unsigned p = n;                             // next one at or after n
+      while (p < (unsigned)N) {
+        const uint64_t w = pl[p >> 6] >> (p & 63);
+        if (w) { p += ctz64(w); break; }
+        p = (p | 63) + 1;
+      }
+      if (p >= (unsigned)N) { out.put(0, 1); break; }
+      out.put(1, 1);
+      for (; bits && n < (unsigned)N - 1; n++) {
+        bits--;
+        const unsigned b = n == p;
+        out.put(b, 1);
+        if (b) break;
+      }
+      n++;
+    }
+  }
+  return budget - bits;
+}
+
+template <typename U, class Source>
+ZG_HD unsigned decode_planes_wide(Source& in, unsigned budget, unsigned maxprec, U (&u)[256]) {
+  constexpr int P = 8 * sizeof(U), N = 256;
+  const int kmin = (unsigned)P > maxprec ? P - (int)maxprec : 0;
+  unsigned bits = budget, n = 0;
+  for (int i = 0; i < N; i++) u[i] = 0;
+  for (int k = P - 1; k >= kmin && bits; k--) {
+    const unsigned m = n < bits ? n : bits;
+    for (unsigned i = 0; i < m; i += 64) {
+      const unsigned c = m - i < 64 ? m - i : 64;
+      const uint64_t v = in.read(c);
+      for (unsigned j = 0; j < c; j++) u[i + j] += (U)((v >> j) & 1u) << k;
+    }
+    bits -= m;
+    while (bits && n < (unsigned)N) {
+      bits--;
+      if (!in.read(1)) break;
+      for (; bits && n < (unsigned)N - 1; n++) {
+        bits--;
+        if (in.read(1)) break;
+      }
+      u[n] += (U)1 << k;
+      n++;
+    }
+  }
+  return budget - bits;
+}
+
+// ---------------------------------------------------------------------------
+// integer block codec (src/template/encode.c:260-280, decode.c:282-298,
+// revencode.c:57-79, revdecode.c:37-55)
+
+template <int D, typename I, class Source>
+ZG_HD unsigned uncode_coeffs(Source& in, unsigned budget, unsigned maxprec,
+                             typename std::make_unsigned<I>::type (&u)[1 << (2 * D)]) {
+  using U = typename std::make_unsigned<I>::type;
+  constexpr int N = 1 << (2 * D);
+  if constexpr (N <= 64) {
+    uint64_t pl[8 * sizeof(U)];
+    const unsigned bits = decode_planes<8 * sizeof(U), N>(in, budget, maxprec, pl);
+    take_planes<N>(pl, u);
+    return bits;
+  } else {
+    return decode_planes_wide<U>(in, budget, maxprec, u);
+  }
+}
+
+template <int D, typename I, class Source>
+ZG_HD unsigned decode_ints(Source& in, unsigned minbits, unsigned maxbits, unsigned maxprec,
+                           I (&v)[1 << (2 * D)]) {
+  using U = typename std::make_unsigned<I>::type;
+  constexpr int N = 1 << (2 * D);
+  U u[N];
+  unsigned bits = uncode_coeffs<D, I>(in, maxbits, maxprec, u);
+  if (bits < minbits) { in.skip_long(minbits - bits); bits = minbits; }
+#pragma unroll (N <= 64 ? N : 1)
+  for (int i = 0; i < N; i++) v[perm<D>(i)] = from_nb<I>(u[i]);
+  xform<kInv, D>(v);
+  return bits;
+}
+
+template <int D, typename I, class Source>
+ZG_HD unsigned rev_decode_ints(Source& in, unsigned minbits, unsigned maxbits, I (&v)[1 << (2 * D)]) {
+  using U = typename std::make_unsigned<I>::type;
+  constexpr int N = 1 << (2 * D);
+  constexpr unsigned kPBits = sizeof(I) == 4 ? 5 : 6;
+  const unsigned prec = (unsigned)in.read(kPBits) + 1;
+  U u[N];
+  unsigned bits = kPBits + uncode_coeffs<D, I>(in, maxbits - kPBits, prec, u);
+  if (bits < minbits) { in.skip_long(minbits - bits); bits = minbits; }
+#pragma unroll (N <= 64 ? N : 1)
+  for (int i = 0; i < N; i++) v[perm<D>(i)] = from_nb<I>(u[i]);
+  xform<kRevInv, D>(v);
+  return bits;
+}
+
+// ---------------------------------------------------------------------------
+// whole-block front ends.  `raw` holds the gathered block as bit patterns.
+
+ZG_HD unsigned umin(unsigned a, unsigned b) { return a < b ? a : b; }
+
+template <typename S, int D, class Source>
+ZG_HD unsigned decode_float_lossy(Source& in, const BlockParams& p,
+                                  typename Traits<S>::Bits (&raw)[1 << (2 * D)]) {
+  using T = Traits<S>;
+  constexpr int N = 1 << (2 * D);
+  unsigned bits = 1;
+  if (in.read(1)) {
+    bits += T::kEBits;
+    const int emax = (int)in.read(T::kEBits) - T::kEBias;
+    const unsigned maxprec = coded_precision(emax, p.maxprec, p.minexp, D);
+    typename T::Int v[N];
+    bits += decode_ints<D>(in, p.minbits - umin(bits, p.minbits), p.maxbits - bits, maxprec, v);
+    inv_cast<S, N>(v, raw, emax);
+  } else {
+#pragma unroll (N <= 64 ? N : 1)
+    for (int i = 0; i < N; i++) raw[i] = 0;
+    if (p.minbits > bits) { in.skip_long(p.minbits - bits); bits = p.minbits; }
+  }
+  return bits;
+}
+
+template <typename S, int D, class Source>
+ZG_HD unsigned decode_float_rev(Source& in, const BlockParams& p,
+                                typename Traits<S>::Bits (&raw)[1 << (2 * D)]) {
+  using T = Traits<S>;
+  using B = typename T::Bits;
+  using I = typename T::Int;
+  constexpr int N = 1 << (2 * D);
+  constexpr B kTc = ~(B(1) << (8 * sizeof(B) - 1));
+  unsigned bits = 1;
+  if (in.read(1)) {
+    I v[N];
+    bits++;
+    if (in.read(1)) {
+      bits += rev_decode_ints<D>(in, p.minbits - umin(bits, p.minbits), p.maxbits - bits, v);
+#pragma unroll (N <= 64 ? N : 1)
+      for (int i = 0; i < N; i++) raw[i] = v[i] < 0 ? ((B)v[i] ^ kTc) : (B)v[i];
+    } else {
+      bits += T::kEBits;
+      const int emax = (int)in.read(T::kEBits) - T::kEBias;
+      bits += rev_decode_ints<D>(in, p.minbits - umin(bits, p.minbits), p.maxbits - bits, v);
+      if (emax != -T::kEBias) inv_cast<S, N>(v, raw, emax);
+      else
+        for (int i = 0; i < N; i++) raw[i] = 0;
+    }
+  } else {
+#pragma unroll (N <= 64 ? N : 1)
+    for (int i = 0; i < N; i++) raw[i] = 0;
+    if (p.minbits > bits) { in.skip_long(p.minbits - bits); bits = p.minbits; }
+  }
+  return bits;
+}
+
+// ---------------------------------------------------------------------------
+// encoder: a block is first prepared (header, coding budget and bit planes
+// held in registers) and then emitted.  Kernels that need the block's length
+// before writing it (variable-rate streams) run length() between the two.
+
+struct CountSink {
+  unsigned n = 0;
+  ZG_HD void put(uint64_t, unsigned k) { n += k; }
+  ZG_HD void pad(unsigned k) { n += k; }
+};
+
+template <typename S, int D>
+struct BlockCode {
+  using U = typename Traits<S>::UInt;
+  static constexpr int N = 1 << (2 * D);
+  static constexpr int P = 8 * sizeof(U);
+  static constexpr bool kWide = N > 64;
+  uint64_t hdr;        // header bits, first bit in the LSB
+  unsigned hdr_bits;
+  unsigned budget;     // bits granted to the plane coder (unsigned wrap as in the reference)
+  unsigned maxprec;    // bit planes to code
+  unsigned pad_to;     // the block is padded with zeros to at least this many bits
+  bool coded;          // false: header only
+  typename std::conditional<kWide, U[N], uint64_t[P]>::type data;  // planes, or coefficients for 4D
+
+  template <class Sink>
+  ZG_HD unsigned emit(Sink& out) const {
+    out.put(hdr, hdr_bits);
+    unsigned bits = hdr_bits;
+    if (coded) {
+      if constexpr (kWide) bits += encode_planes_wide<U>(out, budget, maxprec, data);
+      else bits += encode_planes<P, N>(out, budget, maxprec, data);
+    }
+    if (bits < pad_to) { out.pad(pad_to - bits); bits = pad_to; }
+    return bits;
+  }
+  ZG_HD unsigned length() const {
+    CountSink c;
+    return emit(c);
+  }
+};
+
+// reorder by sequency and map to negabinary (src/template/encode.c:83-88)
+template <int D, typename I>
+ZG_HD void reorder(const I (&v)[1 << (2 * D)], typename std::make_unsigned<I>::type (&u)[1 << (2 * D)]) {
+  constexpr int N = 1 << (2 * D);
+#pragma unroll (N <= 64 ? N : 1)
+  for (int i = 0; i < N; i++) u[i] = to_nb<I>(v[perm<D>(i)]);
+}
+
+template <typename S, int D>
+ZG_HD void set_coeffs(BlockCode<S, D>& bc, const typename Traits<S>::UInt (&u)[1 << (2 * D)]) {
+  constexpr int N = 1 << (2 * D);
+  if constexpr (BlockCode<S, D>::kWide) {
+    for (int i = 0; i < N; i++) bc.data[i] = u[i];
+  } else {
+    make_planes<N>(u, bc.data);
+  }
+}
+
+// precision of a reversible block: top plane down to the lowest set bit of
+// any coefficient (src/template/revencode.c:37-53), clamped to [1, maxprec]
+template <typename U, int N>
+ZG_HD unsigned rev_precision(const U (&u)[N], unsigned maxprec) {
+  U all = 0;
+#pragma unroll (N <= 64 ? N : 1)
+  for (int i = 0; i < N; i++) all |= u[i];
+  unsigned prec = all ? 8 * sizeof(U) - ctz64((uint64_t)all) : 0;
+  if (prec > maxprec) prec = maxprec;
+  if (prec < 1) prec = 1;
+  return prec;
+}
+
+// Prepare one gathered block of scalar type S (bit patterns in `raw`).
+// Lossy floating point: src/template/encodef.c:63-90; reversible floating
+// point: revencodef.c:45-80; integers: encode.c:260-280, revencode.c:57-79.
+template <typename S, int D>
+ZG_HD void prepare_block(BlockCode<S, D>& bc, const BlockParams& p,
+                         const typename Traits<S>::Bits (&raw)[1 << (2 * D)]) {
+  using T = Traits<S>;
+  using B = typename T::Bits;
+  using I = typename T::Int;
+  using U = typename T::UInt;
+  constexpr int N = 1 << (2 * D);
+  const bool rev = p.minexp < kMinExp;
+  I v[N];
+  U u[N];
+  bc.pad_to = p.minbits;
+  bc.coded = true;
+  if constexpr (T::kFloat) {
+    bool special;
+    const int emax = block_emax<S, N>(raw, special);
+    if (!rev) {
+      const unsigned maxprec = coded_precision(emax, p.maxprec, p.minexp, D);
+      const unsigned e = maxprec ? (unsigned)(emax + T::kEBias) : 0u;
+      if (!e) {                                    // single zero bit, padded to minbits
+        bc.hdr = 0; bc.hdr_bits = 1; bc.coded = false;
+        return;
+      }
+      bc.hdr = 2 * (uint64_t)e + 1;
+      bc.hdr_bits = 1 + T::kEBits;
+      bc.budget = p.maxbits - bc.hdr_bits;
+      bc.maxprec = maxprec;
+      fwd_cast<S, N>(raw, v, emax, special);
+      xform<kFwd, D>(v);
+      reorder<D>(v, u);
+      set_coeffs(bc, u);
+      return;
+    }
+    constexpr B kTc = ~(B(1) << (8 * sizeof(B) - 1));
+    bool exact = true;
+    if (emax != -T::kEBias) {
+      fwd_cast<S, N>(raw, v, emax, special);
+      const S s = pow2<S>(emax - (T::kPrec - 2));
+#pragma unroll (N <= 64 ? N : 1)
+      for (int i = 0; i < N; i++) exact &= to_bits<S>(fmul<S>(s, int_to_float<S>(v[i]))) == raw[i];
+    } else {
+#pragma unroll (N <= 64 ? N : 1)
+      for (int i = 0; i < N; i++) { v[i] = 0; exact &= raw[i] == 0; }
+    }
+    unsigned outer;
+    if (exact) {
+      const unsigned e = (unsigned)(emax + T::kEBias);
+      if (!e) {                                    // all-zero block: one bit, never padded
+        bc.hdr = 0; bc.hdr_bits = 1; bc.coded = false; bc.pad_to = 0;
+        return;
+      }
+      bc.hdr = 1 | ((uint64_t)e << 2);
+      outer = 2 + T::kEBits;
+    } else {                                       // reinterpret sign-magnitude as two's complement
+#pragma unroll (N <= 64 ? N : 1)
+      for (int i = 0; i < N; i++) v[i] = (I)raw[i] < 0 ? (I)(raw[i] ^ kTc) : (I)raw[i];
+      bc.hdr = 3;
+      outer = 2;
+    }
+    xform<kRevFwd, D>(v);
+    reorder<D>(v, u);
+    const unsigned prec = rev_precision<U, N>(u, p.maxprec);
+    bc.hdr |= (uint64_t)(prec - 1) << outer;
+    bc.hdr_bits = outer + T::kPBits;
+    bc.budget = p.maxbits - outer - T::kPBits;
+    bc.maxprec = prec;
+    set_coeffs(bc, u);
+  } else {
+#pragma unroll (N <= 64 ? N : 1)
+    for (int i = 0; i < N; i++) v[i] = (I)raw[i];
+    if (!rev) {
+      bc.hdr = 0; bc.hdr_bits = 0;
+      bc.budget = p.maxbits;
+      bc.maxprec = p.maxprec;
+      xform<kFwd, D>(v);
+      reorder<D>(v, u);
+      set_coeffs(bc, u);
+    } else {
+      xform<kRevFwd, D>(v);
+      reorder<D>(v, u);
+      const unsigned prec = rev_precision<U, N>(u, p.maxprec);
+      bc.hdr = prec - 1;
+      bc.hdr_bits = T::kPBits;
+      bc.budget = p.maxbits - T::kPBits;
+      bc.maxprec = prec;
+      set_coeffs(bc, u);
+    }
+  }
+}
+
+template <typename S, int D, class Sink>
+ZG_HD unsigned encode_block(Sink& out, const BlockParams& p, const typename Traits<S>::Bits (&raw)[1 << (2 * D)]) {
+  BlockCode<S, D> bc;
+  prepare_block<S, D>(bc, p, raw);
+  return bc.emit(out);
+}
+
+template <typename S, int D, class Source>
+ZG_HD unsigned decode_block(Source& in, const BlockParams& p, typename Traits<S>::Bits (&raw)[1 << (2 * D)]) {
+  using T = Traits<S>;
+  constexpr int N = 1 << (2 * D);
+  const bool rev = p.minexp < kMinExp;
+  if constexpr (T::kFloat) {
+    return rev ? decode_float_rev<S, D>(in, p, raw) : decode_float_lossy<S, D>(in, p, raw);
+  } else {
+    typename T::Int v[N];
+    const unsigned bits = rev ? rev_decode_ints<D>(in, p.minbits, p.maxbits, v)
+                              : decode_ints<D>(in, p.minbits, p.maxbits, p.maxprec, v);
+#pragma unroll (N <= 64 ? N : 1)
+    for (int i = 0; i < N; i++) raw[i] = (typename T::Bits)v[i];
+    return bits;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// bit source over a word array: a 128-bit window, loads past `cap` words
+// read as zero so a corrupt or truncated stream cannot fault.  kGlobal
+// selects read-only global loads; otherwise plain (e.g. shared-memory) loads.
+
+template <bool kGlobal>
+struct WordSourceT {
+  const uint64_t* base;
+  uint64_t cap;     // readable words
+  uint64_t at;      // absolute position of the next bit
+  uint64_t next;    // index of the next word to load
+  uint64_t lo, hi;
+  unsigned pos;     // bit offset of `at` inside lo
+
+  ZG_HD uint64_t load(uint64_t i) const {
+#if defined(__CUDA_ARCH__)
+    if constexpr (kGlobal) return i < cap ? __ldg((const unsigned long long*)base + i) : 0ull;
+    else return i < cap ? base[i] : 0ull;
+#else
+    return i < cap ? base[i] : 0ull;
+#endif
+  }
+  ZG_HD void seek(uint64_t bit) {
+    at = bit;
+    const uint64_t w = bit >> 6;
+    lo = load(w);
+    hi = load(w + 1);
+    next = w + 2;
+    pos = (unsigned)(bit & 63);
+  }
+  ZG_HD uint64_t peek(unsigned n) const {     // n <= 64
+    const uint64_t w = pos ? (lo >> pos) | (hi << (64 - pos)) : lo;
+    return low_bits(w, n);
+  }
+  ZG_HD void skip(unsigned n) {               // n <= 64
+    at += n;
+    pos += n;
+    if (pos >= 64) {
+      lo = hi;
+      hi = load(next++);
+      pos -= 64;
+    }
+  }
+  ZG_HD uint64_t read(unsigned n) {
+    const uint64_t v = peek(n);
+    skip(n);
+    return v;
+  }
+  ZG_HD void skip_long(uint64_t n) { seek(at + n); }
+};
+
+using WordSource = WordSourceT<true>;
+using SharedSource = WordSourceT<false>;
+
+}  // namespace zg

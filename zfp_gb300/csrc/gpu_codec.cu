@@ -1,0 +1,707 @@
+// gpu_codec.cu -- zfp_compress / zfp_decompress on the GPU.
+//
+// The reference's CUDA hook (src/cuda_zfp/cuZFP.cu:357-491) accepted only
+// fixed-rate 1-3D contiguous fields; this path takes every mode, type,
+// dimensionality, stride layout and stream offset the serial codec takes
+// (src/zfp.c:1052-1180) and produces the same bits.  Per call:
+//   1. classify field and stream buffers (host or device); stage host data
+//      through device memory from the stream-ordered pool;
+//   2. describe the field as one Job and launch the encode/decode kernel on
+//      the zfp_stream's CUDA stream;
+//   3. leave the bit stream as the serial path leaves it (flushed on
+//      compress, aligned on decompress) and return the byte size.
+// Variable-rate streams carry no block index (docs/source/execution.rst:289-
+// 300); the encoder records one in device memory, kept in a small registry
+// keyed by stream buffer and start bit, and the decoder verifies it.  For a
+// stream with no entry (written elsewhere) the offsets are recovered on the
+// GPU by a sequential parse.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/zfp_gb300.h"
+#include "job.h"
+#include "launch.h"
+#include "runtime.h"
+
+namespace zg {
+
+// ---------------------------------------------------------------------------
+// errors and per-stream GPU settings
+
+static thread_local std::string g_last_error;
+
+void set_error(const char* msg) { g_last_error = msg ? msg : ""; }
+
+static size_t fail(const char* msg) {
+  set_error(msg);
+  return 0;
+}
+
+static size_t fail_cuda(const char* where, cudaError_t e) {
+  std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+  set_error(m.c_str());
+  return 0;
+}
+
+struct ExecParams {
+  uint32_t magic;
+  cudaStream_t stream;
+  int async;
+};
+static const uint32_t kExecMagic = 0x7a673330u;  // identifies params owned by this library
+
+bool ensure_exec_params(zfp_stream* z) {
+  if (z->exec.policy == zfp_exec_cuda && z->exec.params) return true;
+  if (z->exec.params) std::free(z->exec.params);
+  ExecParams* p = (ExecParams*)std::malloc(sizeof(ExecParams));
+  if (!p) return false;
+  p->magic = kExecMagic;
+  p->stream = nullptr;
+  p->async = 0;
+  z->exec.params = p;
+  return true;
+}
+
+void release_exec_params(zfp_stream* z) {
+  if (z->exec.params) std::free(z->exec.params);
+  z->exec.params = nullptr;
+}
+
+static ExecParams* exec_params(zfp_stream* z) {
+  ExecParams* p = (ExecParams*)z->exec.params;
+  return (p && p->magic == kExecMagic) ? p : nullptr;
+}
+
+// ---------------------------------------------------------------------------
+// memory
+
+static bool is_device_ptr(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+static void init_pool_once() {
+  static std::once_flag flag;
+  std::call_once(flag, [] {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t keep = ~0ull;  // keep freed blocks for reuse instead of returning them
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+  });
+}
+
+// stream-ordered device buffer
+struct DevBuf {
+  void* p = nullptr;
+  cudaStream_t st = nullptr;
+  cudaError_t alloc(size_t bytes, cudaStream_t s) {
+    st = s;
+    return cudaMallocAsync(&p, bytes ? bytes : 8, s);
+  }
+  void release() {
+    if (p) cudaFreeAsync(p, st);
+    p = nullptr;
+  }
+  ~DevBuf() { release(); }
+};
+
+// ---------------------------------------------------------------------------
+// field description
+
+struct FieldInfo {
+  int type = 0, dims = 0;
+  size_t esize = 0;
+  uint32_t n[4] = {1, 1, 1, 1}, nb[4] = {1, 1, 1, 1};
+  int64_t s[4] = {0, 0, 0, 0};
+  uint64_t nblocks = 0;
+  ptrdiff_t lo = 0, hi = 0;  // lowest / highest element offset
+};
+
+static const char* field_info(const zfp_field* f, FieldInfo& fi) {
+  switch (f->type) {
+    case zfp_type_int32: case zfp_type_float: fi.esize = 4; break;
+    case zfp_type_int64: case zfp_type_double: fi.esize = 8; break;
+    default: return "unsupported scalar type";
+  }
+  fi.type = f->type;
+  fi.dims = f->nx ? f->ny ? f->nz ? f->nw ? 4 : 3 : 2 : 1 : 0;
+  if (!fi.dims) return "field has no dimensions";
+  const size_t n[4] = {f->nx, f->ny, f->nz, f->nw};
+  const ptrdiff_t sd[4] = {f->sx ? f->sx : 1, f->sy ? f->sy : (ptrdiff_t)f->nx,
+                           f->sz ? f->sz : (ptrdiff_t)(f->nx * f->ny),
+                           f->sw ? f->sw : (ptrdiff_t)(f->nx * f->ny * f->nz)};
+  fi.nblocks = 1;
+  for (int a = 0; a < 4; a++) {
+    if (a < fi.dims) {
+      if (n[a] >= (1ull << 32) - 4) return "field extent too large";
+      fi.n[a] = (uint32_t)n[a];
+      fi.nb[a] = (fi.n[a] + 3) / 4;
+      fi.s[a] = sd[a];
+      const ptrdiff_t d = sd[a] * (ptrdiff_t)(n[a] - 1);
+      fi.lo += d < 0 ? d : 0;
+      fi.hi += d > 0 ? d : 0;
+    }
+    fi.nblocks *= fi.nb[a];
+  }
+  if (!f->data) return "field has no data pointer";
+  return nullptr;
+}
+
+// header bits a block can carry before its bit planes
+static uint32_t header_max(int type, bool rev) {
+  switch (type) {
+    case zfp_type_int32: return rev ? 5 : 0;
+    case zfp_type_int64: return rev ? 6 : 0;
+    case zfp_type_float: return rev ? 1 + 1 + 8 + 5 : 1 + 8;
+    default: return rev ? 1 + 1 + 11 + 6 : 1 + 11;
+  }
+}
+
+// upper bound on the bits of one block (the block term of
+// zfp_stream_maximum_size, src/zfp.c:712-742, widened where a maxbits
+// below the header size makes the reference's budget wrap around)
+static uint64_t block_bound(const FieldInfo& fi, const zfp_stream* z) {
+  const bool rev = z->minexp < ZFP_MIN_EXP;
+  const uint64_t values = 1ull << (2 * fi.dims);
+  const uint64_t prec = 8 * fi.esize;
+  const uint64_t hm = header_max(fi.type, rev);
+  const uint64_t coder = values - 1 + values * std::min<uint64_t>(z->maxprec, prec);
+  uint64_t b = hm + coder;
+  if (z->maxbits >= hm) b = std::min<uint64_t>(b, z->maxbits);
+  return std::max<uint64_t>(b, z->minbits);
+}
+
+static bool is_fixed_rate(const FieldInfo& fi, const zfp_stream* z) {
+  const bool rev = z->minexp < ZFP_MIN_EXP;
+  return !rev && z->minbits == z->maxbits && z->maxbits >= header_max(fi.type, false) && z->maxbits > 0;
+}
+
+static bool vector_ok(const FieldInfo& fi, const void* data) {
+  if (fi.s[0] != 1 || ((uintptr_t)data & 15)) return false;
+  for (int a = 1; a < fi.dims; a++)
+    if ((fi.s[a] * (int64_t)fi.esize) % 16) return false;
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// index registry for variable-rate streams
+
+struct IndexEntry {
+  const void* begin;
+  uint64_t bit0, end_bit, nblocks;
+  int type, dims;
+  uint32_t minbits, maxbits, maxprec;
+  int32_t minexp;
+  uint64_t* offsets;       // device, nblocks words
+  cudaStream_t stream;     // last stream that used it (frees are ordered after it)
+  uint64_t tick;
+};
+
+static std::mutex g_reg_mu;
+static std::vector<IndexEntry> g_reg;
+static uint64_t g_tick = 0;
+static const size_t kRegistryBytes = 4ull << 30;
+
+static void free_entry(IndexEntry& e) {
+  if (!e.offsets) return;
+  if (cudaFreeAsync(e.offsets, e.stream) != cudaSuccess) {
+    cudaGetLastError();
+    cudaDeviceSynchronize();
+    cudaFree(e.offsets);
+  }
+  e.offsets = nullptr;
+}
+
+// drop entries of the same buffer whose stream range overlaps [bit0, end)
+static void registry_invalidate(const void* begin, uint64_t bit0, uint64_t end) {
+  std::lock_guard<std::mutex> lk(g_reg_mu);
+  for (size_t i = 0; i < g_reg.size();) {
+    IndexEntry& e = g_reg[i];
+    if (e.begin == begin && e.bit0 < end && bit0 < e.end_bit) {
+      free_entry(e);
+      g_reg.erase(g_reg.begin() + i);
+    } else {
+      i++;
+    }
+  }
+}
+
+static void registry_insert(const IndexEntry& ne) {
+  registry_invalidate(ne.begin, ne.bit0, ne.end_bit);
+  std::lock_guard<std::mutex> lk(g_reg_mu);
+  size_t bytes = ne.nblocks * 8;
+  for (auto& e : g_reg) bytes += e.nblocks * 8;
+  while (bytes > kRegistryBytes && !g_reg.empty()) {
+    auto it = std::min_element(g_reg.begin(), g_reg.end(),
+                               [](const IndexEntry& a, const IndexEntry& b) { return a.tick < b.tick; });
+    bytes -= it->nblocks * 8;
+    free_entry(*it);
+    g_reg.erase(it);
+  }
+  g_reg.push_back(ne);
+  g_reg.back().tick = ++g_tick;
+}
+
+static bool registry_find(const void* begin, uint64_t bit0, const FieldInfo& fi, const zfp_stream* z,
+                          cudaStream_t st, IndexEntry& out) {
+  std::lock_guard<std::mutex> lk(g_reg_mu);
+  for (auto& e : g_reg)
+    if (e.begin == begin && e.bit0 == bit0 && e.nblocks == fi.nblocks && e.type == fi.type &&
+        e.dims == fi.dims && e.minbits == z->minbits && e.maxbits == z->maxbits && e.maxprec == z->maxprec &&
+        e.minexp == z->minexp) {
+      e.tick = ++g_tick;
+      e.stream = st;
+      out = e;
+      return true;
+    }
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+// launch helpers
+
+static Job base_job(const FieldInfo& fi, const zfp_stream* z, void* field) {
+  Job j;
+  std::memset(&j, 0, sizeof j);
+  j.field = field;
+  for (int a = 0; a < 4; a++) {
+    j.s[a] = fi.s[a];
+    j.n[a] = fi.n[a];
+    j.nb[a] = fi.nb[a];
+  }
+  j.nblocks = fi.nblocks;
+  j.minbits = z->minbits;
+  j.maxbits = z->maxbits;
+  j.maxprec = z->maxprec;
+  j.minexp = z->minexp;
+  j.tile0 = 0;
+  j.ntiles = (uint32_t)((fi.nblocks + kTile - 1) / kTile);
+  return j;
+}
+
+static int persistent_grid() {
+  static int sms = [] {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 148;
+  }();
+  return sms * 4;
+}
+
+// decide shared- or global-memory staging and the grid
+static cudaError_t plan_launch(LaunchArgs& a, uint64_t bound_bits, uint32_t total_tiles, DevBuf& gimg,
+                               cudaStream_t st) {
+  const uint64_t words = (uint64_t)kTile * bound_bits / 64 + 4;
+  a.total_tiles = total_tiles;
+  a.img_words = (uint32_t)words;
+  a.gimg = nullptr;
+  a.grid = (int)total_tiles;
+  if (words * 8 > kMaxTileSmem) {
+    a.grid = (int)std::min<uint64_t>(total_tiles, (uint64_t)persistent_grid());
+    cudaError_t e = gimg.alloc((size_t)a.grid * words * 8, st);
+    if (e != cudaSuccess) return e;
+    a.gimg = (uint64_t*)gimg.p;
+  }
+  return cudaSuccess;
+}
+
+static cudaError_t launch_encode_any(int type, int dims, const LaunchArgs& a, cudaStream_t st) {
+  switch (type) {
+    case zfp_type_int32: return launch_encode_i32(dims, a, st);
+    case zfp_type_int64: return launch_encode_i64(dims, a, st);
+    case zfp_type_float: return launch_encode_f32(dims, a, st);
+    default: return launch_encode_f64(dims, a, st);
+  }
+}
+
+static cudaError_t launch_decode_any(int type, int dims, const LaunchArgs& a, cudaStream_t st) {
+  switch (type) {
+    case zfp_type_int32: return launch_decode_i32(dims, a, st);
+    case zfp_type_int64: return launch_decode_i64(dims, a, st);
+    case zfp_type_float: return launch_decode_f32(dims, a, st);
+    default: return launch_decode_f64(dims, a, st);
+  }
+}
+
+static cudaError_t launch_parse_any(int type, int dims, const Job& j, cudaStream_t st) {
+  switch (type) {
+    case zfp_type_int32: return launch_parse_i32(dims, j, st);
+    case zfp_type_int64: return launch_parse_i64(dims, j, st);
+    case zfp_type_float: return launch_parse_f32(dims, j, st);
+    default: return launch_parse_f64(dims, j, st);
+  }
+}
+
+// scratch for one launch: result slot + look-back / boundary state, zeroed
+struct LaunchMem {
+  DevBuf buf;
+  JobResult* result = nullptr;
+  LaunchScratch sc{};
+  cudaError_t make(uint32_t total_tiles, cudaStream_t st) {
+    const size_t t = (size_t)total_tiles + 1;
+    const size_t bytes = 64 + t * 8 + t * 16 + t * 4 + 16;
+    cudaError_t e = buf.alloc(bytes, st);
+    if (e != cudaSuccess) return e;
+    char* p = (char*)buf.p;
+    result = (JobResult*)p;
+    sc.ticket = (unsigned int*)(p + 32);
+    sc.tile_state = (unsigned long long*)(p + 64);
+    sc.side = (unsigned long long*)(p + 64 + t * 8);
+    sc.side_cnt = (unsigned int*)(p + 64 + t * 24);
+    return cudaMemsetAsync(p, 0, bytes, st);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// compress
+
+size_t gpu_compress(zfp_stream* z, const zfp_field* f) {
+  ExecParams* ep = exec_params(z);
+  if (!ep) return fail("zfp_compress: stream has no GPU execution parameters");
+  if (!z->stream) return fail("zfp_compress: no bit stream");
+  FieldInfo fi;
+  if (const char* why = field_info(f, fi)) return fail(why);
+  init_pool_once();
+  const cudaStream_t st = ep->stream;
+  const StreamState ss = get_stream_state(z->stream);
+  if (!ss.begin) return fail("zfp_compress: bit stream has no buffer");
+  const uint64_t bit0 = (uint64_t)(ss.ptr - ss.begin) * 64 + ss.bits;
+  const uint64_t cap_words = (uint64_t)(ss.end - ss.begin);
+  const bool fixed = is_fixed_rate(fi, z);
+  const uint64_t bound = block_bound(fi, z);
+  const uint64_t max_end = bit0 + fi.nblocks * (fixed ? (uint64_t)z->maxbits : bound);
+  if (fixed && (max_end + 63) / 64 > cap_words) return fail("zfp_compress: stream buffer too small");
+
+  const bool field_dev = is_device_ptr(f->data);
+  const bool stream_dev = is_device_ptr(ss.begin);
+  cudaError_t e;
+
+  // field
+  DevBuf fstage;
+  void* dfield = f->data;
+  if (!field_dev) {
+    const size_t span = (size_t)(fi.hi - fi.lo + 1) * fi.esize;
+    if ((e = fstage.alloc(span, st)) != cudaSuccess) return fail_cuda("zfp_compress: staging alloc", e);
+    const char* src = (const char*)f->data + fi.lo * (ptrdiff_t)fi.esize;
+    if ((e = cudaMemcpyAsync(fstage.p, src, span, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+      return fail_cuda("zfp_compress: field upload", e);
+    dfield = (char*)fstage.p - fi.lo * (ptrdiff_t)fi.esize;
+  }
+
+  // stream words
+  DevBuf sstage;
+  uint64_t* dwords = ss.begin;
+  uint64_t dcap = cap_words;
+  const uint64_t w_first = bit0 / 64;
+  if (!stream_dev) {
+    const uint64_t w_end = std::min<uint64_t>(cap_words, (max_end + 63) / 64);
+    const uint64_t nw = w_end > w_first ? w_end - w_first : 0;
+    if ((e = sstage.alloc(nw * 8, st)) != cudaSuccess) return fail_cuda("zfp_compress: staging alloc", e);
+    dwords = (uint64_t*)sstage.p - w_first;
+    dcap = w_first + nw;
+  }
+
+  Job job = base_job(fi, z, dfield);
+  job.flags = (fixed ? kFixedRate : 0u) | (vector_ok(fi, dfield) ? kVecOk : 0u);
+  job.words = dwords;
+  job.cap_words = dcap;
+  job.bit0 = bit0;
+  job.head_word = ss.bits ? (ss.buffer & ((1ull << ss.bits) - 1)) : 0;
+
+  uint64_t* offsets = nullptr;
+  if (!fixed) {
+    if ((e = cudaMallocAsync((void**)&offsets, fi.nblocks * 8, st)) != cudaSuccess)
+      return fail_cuda("zfp_compress: index alloc", e);
+    job.offsets = offsets;
+    job.flags |= kWriteIndex;
+  }
+
+  LaunchMem lm;
+  if ((e = lm.make(job.ntiles, st)) != cudaSuccess) {
+    if (offsets) cudaFreeAsync(offsets, st);
+    return fail_cuda("zfp_compress: scratch", e);
+  }
+  job.result = lm.result;
+
+  LaunchArgs a;
+  std::memset(&a, 0, sizeof a);
+  a.one = job;
+  a.njobs = 1;
+  a.sc = lm.sc;
+  a.use_ticket = fixed ? 0 : 1;
+  DevBuf gimg;
+  if ((e = plan_launch(a, fixed ? z->maxbits : bound, job.ntiles, gimg, st)) != cudaSuccess ||
+      (e = launch_encode_any(fi.type, fi.dims, a, st)) != cudaSuccess) {
+    if (offsets) cudaFreeAsync(offsets, st);
+    return fail_cuda("zfp_compress: launch", e);
+  }
+
+  if (fixed && field_dev && stream_dev && ep->async) {
+    const uint64_t end = bit0 + fi.nblocks * (uint64_t)z->maxbits;
+    registry_invalidate(ss.begin, bit0, end);
+    set_stream_flushed(z->stream, end);
+    return (size_t)((end + 63) / 64) * 8;
+  }
+
+  JobResult res;
+  if ((e = cudaMemcpyAsync(&res, lm.result, sizeof res, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+    if (offsets) cudaFreeAsync(offsets, st);
+    return fail_cuda("zfp_compress: kernel", e);
+  }
+  if (res.status) {
+    if (offsets) cudaFreeAsync(offsets, st);
+    return fail(res.status & kStatusOverflow ? "zfp_compress: stream buffer too small"
+                                             : "zfp_compress: GPU wait timed out");
+  }
+  const uint64_t end = res.end_bit;
+  if (!stream_dev) {
+    const uint64_t w_end = (end + 63) / 64;
+    if ((e = cudaMemcpyAsync(ss.begin + w_first, dwords + w_first, (w_end - w_first) * 8, cudaMemcpyDeviceToHost,
+                             st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+      if (offsets) cudaFreeAsync(offsets, st);
+      return fail_cuda("zfp_compress: stream download", e);
+    }
+  }
+  if (offsets) {
+    IndexEntry ne;
+    ne.begin = ss.begin;
+    ne.bit0 = bit0;
+    ne.end_bit = end;
+    ne.nblocks = fi.nblocks;
+    ne.type = fi.type;
+    ne.dims = fi.dims;
+    ne.minbits = z->minbits;
+    ne.maxbits = z->maxbits;
+    ne.maxprec = z->maxprec;
+    ne.minexp = z->minexp;
+    ne.offsets = offsets;
+    ne.stream = st;
+    ne.tick = 0;
+    registry_insert(ne);
+  } else {
+    registry_invalidate(ss.begin, bit0, end);
+  }
+  set_stream_flushed(z->stream, end);
+  set_error("");
+  return (size_t)((end + 63) / 64) * 8;
+}
+
+// ---------------------------------------------------------------------------
+// decompress
+
+size_t gpu_decompress(zfp_stream* z, zfp_field* f) {
+  ExecParams* ep = exec_params(z);
+  if (!ep) return fail("zfp_decompress: stream has no GPU execution parameters");
+  if (!z->stream) return fail("zfp_decompress: no bit stream");
+  FieldInfo fi;
+  if (const char* why = field_info(f, fi)) return fail(why);
+  init_pool_once();
+  const cudaStream_t st = ep->stream;
+  const StreamState ss = get_stream_state(z->stream);
+  if (!ss.begin) return fail("zfp_decompress: bit stream has no buffer");
+  const uint64_t bit0 = (uint64_t)(ss.ptr - ss.begin) * 64 - ss.bits;
+  const uint64_t cap_words = (uint64_t)(ss.end - ss.begin);
+  const bool fixed = is_fixed_rate(fi, z);
+  const uint64_t bound = block_bound(fi, z);
+  const bool field_dev = is_device_ptr(f->data);
+  const bool stream_dev = is_device_ptr(ss.begin);
+  cudaError_t e;
+
+  uint64_t end = 0;
+  IndexEntry ent;
+  bool have_index = false;
+  if (fixed) {
+    end = bit0 + fi.nblocks * (uint64_t)z->maxbits;
+    if ((end + 63) / 64 > cap_words) return fail("zfp_decompress: stream shorter than the field");
+  } else {
+    have_index = registry_find(ss.begin, bit0, fi, z, st, ent);
+    if (have_index) end = ent.end_bit;
+  }
+
+  // stream words
+  DevBuf sstage;
+  uint64_t* dwords = ss.begin;
+  uint64_t dcap = cap_words;
+  const uint64_t w_first = bit0 / 64;
+  if (!stream_dev) {
+    const uint64_t w_end = (fixed || have_index) ? std::min<uint64_t>(cap_words, (end + 63) / 64) : cap_words;
+    const uint64_t nw = w_end > w_first ? w_end - w_first : 0;
+    if ((e = sstage.alloc(nw * 8, st)) != cudaSuccess) return fail_cuda("zfp_decompress: staging alloc", e);
+    if (nw && (e = cudaMemcpyAsync(sstage.p, ss.begin + w_first, nw * 8, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+      return fail_cuda("zfp_decompress: stream upload", e);
+    dwords = (uint64_t*)sstage.p - w_first;
+    dcap = w_first + nw;
+  }
+
+  // field
+  DevBuf fstage;
+  void* dfield = f->data;
+  const size_t span = (size_t)(fi.hi - fi.lo + 1) * fi.esize;
+  if (!field_dev) {
+    if ((e = fstage.alloc(span, st)) != cudaSuccess) return fail_cuda("zfp_decompress: staging alloc", e);
+    const uint64_t count = (uint64_t)fi.n[0] * fi.n[1] * fi.n[2] * fi.n[3];
+    if (count * fi.esize != span) {  // strided with gaps: keep what lies between the values
+      const char* src = (const char*)f->data + fi.lo * (ptrdiff_t)fi.esize;
+      if ((e = cudaMemcpyAsync(fstage.p, src, span, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return fail_cuda("zfp_decompress: field upload", e);
+    }
+    dfield = (char*)fstage.p - fi.lo * (ptrdiff_t)fi.esize;
+  }
+
+  Job job = base_job(fi, z, dfield);
+  job.flags = (fixed ? kFixedRate : 0u) | (vector_ok(fi, dfield) ? kVecOk : 0u);
+  job.words = dwords;
+  job.cap_words = dcap;
+  job.bit0 = bit0;
+
+  LaunchMem lm;
+  if ((e = lm.make(job.ntiles, st)) != cudaSuccess) return fail_cuda("zfp_decompress: scratch", e);
+  job.result = lm.result;
+
+  uint64_t* parsed = nullptr;
+  auto parse = [&]() -> cudaError_t {
+    cudaError_t pe;
+    if (!parsed && (pe = cudaMallocAsync((void**)&parsed, fi.nblocks * 8, st)) != cudaSuccess) return pe;
+    Job pj = job;
+    pj.offsets = parsed;
+    if ((pe = launch_parse_any(fi.type, fi.dims, pj, st)) != cudaSuccess) return pe;
+    JobResult r;
+    if ((pe = cudaMemcpyAsync(&r, lm.result, sizeof r, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return pe;
+    if ((pe = cudaStreamSynchronize(st)) != cudaSuccess) return pe;
+    end = r.end_bit;
+    job.offsets = parsed;
+    job.end_bit = end;
+    job.flags &= ~kVerify;
+    return cudaSuccess;
+  };
+
+  if (!fixed) {
+    if (have_index) {
+      job.offsets = ent.offsets;
+      job.end_bit = ent.end_bit;
+      job.flags |= kVerify;
+    } else if ((e = parse()) != cudaSuccess) {
+      if (parsed) cudaFreeAsync(parsed, st);
+      return fail_cuda("zfp_decompress: parse", e);
+    }
+  }
+
+  LaunchArgs a;
+  std::memset(&a, 0, sizeof a);
+  a.njobs = 1;
+  a.sc = lm.sc;
+  DevBuf gimg;
+  if ((e = plan_launch(a, fixed ? z->maxbits : bound, job.ntiles, gimg, st)) != cudaSuccess) {
+    if (parsed) cudaFreeAsync(parsed, st);
+    return fail_cuda("zfp_decompress: plan", e);
+  }
+  a.one = job;
+  if ((e = launch_decode_any(fi.type, fi.dims, a, st)) != cudaSuccess) {
+    if (parsed) cudaFreeAsync(parsed, st);
+    return fail_cuda("zfp_decompress: launch", e);
+  }
+
+  const bool async_ok = fixed && field_dev && stream_dev && ep->async;
+  if (!async_ok) {
+    JobResult res;
+    if ((e = cudaMemcpyAsync(&res, lm.result, sizeof res, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+      if (parsed) cudaFreeAsync(parsed, st);
+      return fail_cuda("zfp_decompress: kernel", e);
+    }
+    if (res.status & kStatusIndex) {
+      // the recorded index does not describe this stream: recover and decode again
+      if ((e = cudaMemsetAsync(lm.result, 0, sizeof(JobResult), st)) != cudaSuccess || (e = parse()) != cudaSuccess) {
+        if (parsed) cudaFreeAsync(parsed, st);
+        return fail_cuda("zfp_decompress: parse", e);
+      }
+      a.one = job;
+      if ((e = launch_decode_any(fi.type, fi.dims, a, st)) != cudaSuccess ||
+          (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+        if (parsed) cudaFreeAsync(parsed, st);
+        return fail_cuda("zfp_decompress: kernel", e);
+      }
+    }
+  }
+  if (!field_dev) {
+    char* dst = (char*)f->data + fi.lo * (ptrdiff_t)fi.esize;
+    if ((e = cudaMemcpyAsync(dst, fstage.p, span, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+      if (parsed) cudaFreeAsync(parsed, st);
+      return fail_cuda("zfp_decompress: field download", e);
+    }
+  }
+  if (parsed) {
+    IndexEntry ne;
+    ne.begin = ss.begin;
+    ne.bit0 = bit0;
+    ne.end_bit = end;
+    ne.nblocks = fi.nblocks;
+    ne.type = fi.type;
+    ne.dims = fi.dims;
+    ne.minbits = z->minbits;
+    ne.maxbits = z->maxbits;
+    ne.maxprec = z->maxprec;
+    ne.minexp = z->minexp;
+    ne.offsets = parsed;
+    ne.stream = st;
+    ne.tick = 0;
+    registry_insert(ne);
+  }
+  set_stream_flushed(z->stream, end);
+  set_error("");
+  return (size_t)((end + 63) / 64) * 8;
+}
+
+}  // namespace zg
+
+// ---------------------------------------------------------------------------
+// extension API (include/zfp_gb300.h)
+
+extern "C" {
+
+zfp_bool zfp_gb300_stream_set_cuda_stream(zfp_stream* z, void* cuda_stream) {
+  if (z->exec.policy != zfp_exec_cuda && !zfp_stream_set_execution(z, zfp_exec_cuda)) return zfp_false;
+  zg::ExecParams* p = zg::exec_params(z);
+  if (!p) return zfp_false;
+  p->stream = (cudaStream_t)cuda_stream;
+  return zfp_true;
+}
+
+zfp_bool zfp_gb300_stream_set_async(zfp_stream* z, int async) {
+  if (z->exec.policy != zfp_exec_cuda && !zfp_stream_set_execution(z, zfp_exec_cuda)) return zfp_false;
+  zg::ExecParams* p = zg::exec_params(z);
+  if (!p) return zfp_false;
+  p->async = async;
+  return zfp_true;
+}
+
+zfp_bool zfp_gb300_stream_synchronize(zfp_stream* z) {
+  zg::ExecParams* p = zg::exec_params(z);
+  cudaError_t e = cudaStreamSynchronize(p ? p->stream : nullptr);
+  if (e != cudaSuccess) {
+    zg::fail_cuda("zfp_gb300_stream_synchronize", e);
+    return zfp_false;
+  }
+  return zfp_true;
+}
+
+const char* zfp_gb300_last_error(void) { return zg::g_last_error.c_str(); }
+
+}  // extern "C"

@@ -1,0 +1,508 @@
+// kernels.cuh -- encode/decode/parse kernels over tiles of zfp blocks.
+//
+// One CTA = one tile of kTile blocks, one block per thread (see codec.cuh).
+//
+// Encode of a tile:
+//   gather (strided, partial blocks padded as src/template/encode.c:9-27)
+//   -> prepare the block in registers -> block length (variable rate only)
+//   -> CTA exclusive scan of lengths -> tile position in the stream:
+//        fixed rate : tile * kTile * maxbits
+//        otherwise  : decoupled look-back over predecessor tiles (bounded
+//                     waits; tiles are handed out in order by a counter so a
+//                     predecessor is always running or finished)
+//   -> every thread writes its block into a shared-memory image of the tile
+//   -> the image is shifted to the stream's bit alignment and stored with
+//      coalesced 64-bit words; the two words a tile shares with its
+//      neighbours are merged through a two-party handshake, never by
+//      zeroing the output first.
+// Decode of a tile: the tile's stream words are staged into shared memory
+// with coalesced loads, each thread decodes its block from there and
+// scatters it.  Block starts come from `block * maxbits` (fixed rate) or the
+// index written at encode time, which the decoder verifies: a block must end
+// exactly where the next one starts, which proves by induction that every
+// recorded start is the true one.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "codec.cuh"
+#include "job.h"
+
+namespace zg {
+
+// ---------------------------------------------------------------------------
+// block coordinates, gather and scatter
+
+__device__ __forceinline__ void block_coords(const Job& job, uint64_t b, uint32_t (&c)[4]) {
+  if (job.nblocks <= 0xffffffffull) {
+    uint32_t r = (uint32_t)b;
+    c[0] = r % job.nb[0]; r /= job.nb[0];
+    c[1] = r % job.nb[1]; r /= job.nb[1];
+    c[2] = r % job.nb[2]; r /= job.nb[2];
+    c[3] = r;
+  } else {
+    uint64_t r = b;
+    c[0] = (uint32_t)(r % job.nb[0]); r /= job.nb[0];
+    c[1] = (uint32_t)(r % job.nb[1]); r /= job.nb[1];
+    c[2] = (uint32_t)(r % job.nb[2]); r /= job.nb[2];
+    c[3] = (uint32_t)r;
+  }
+}
+
+// position i of a partial block row holding cnt valid values reads source
+// index i (i < cnt), else the padding pattern [a], [a b b a], [a b c a]
+__device__ __forceinline__ int pad_index(int i, int cnt) {
+  return i < cnt ? i : (cnt == 2 && i == 2) ? 1 : 0;
+}
+
+template <typename B, int D>
+__device__ __forceinline__ void gather(const Job& job, uint64_t b, B (&raw)[1 << (2 * D)]) {
+  constexpr int N = 1 << (2 * D);
+  constexpr int EX = 4, EY = D >= 2 ? 4 : 1, EZ = D >= 3 ? 4 : 1, EW = D >= 4 ? 4 : 1;
+  uint32_t c[4];
+  block_coords(job, b, c);
+  const int64_t s0 = job.s[0], s1 = job.s[1], s2 = job.s[2], s3 = job.s[3];
+  const B* base = (const B*)job.field + (int64_t)(4 * c[0]) * s0 + (int64_t)(4 * c[1]) * s1 +
+                  (int64_t)(4 * c[2]) * s2 + (int64_t)(4 * c[3]) * s3;
+  int cnt[4];
+  bool full = true;
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    const uint32_t left = job.n[a] - 4 * c[a];
+    cnt[a] = a < D ? (left < 4 ? (int)left : 4) : 1;
+    full &= a >= D || cnt[a] == 4;
+  }
+  if (full && (job.flags & kVecOk)) {
+#pragma unroll (N <= 64 ? N / 4 : 1)
+    for (int r = 0; r < N / 4; r++) {
+      const int y = r & 3, z = (r >> 2) & 3, w = r >> 4;
+      const B* row = base + y * s1 + z * s2 + w * s3;
+      if constexpr (sizeof(B) == 4) {
+        const uint4 q = __ldg((const uint4*)row);
+        raw[4 * r + 0] = q.x; raw[4 * r + 1] = q.y; raw[4 * r + 2] = q.z; raw[4 * r + 3] = q.w;
+      } else {
+        const ulonglong2 q0 = __ldg((const ulonglong2*)row);
+        const ulonglong2 q1 = __ldg((const ulonglong2*)row + 1);
+        raw[4 * r + 0] = q0.x; raw[4 * r + 1] = q0.y; raw[4 * r + 2] = q1.x; raw[4 * r + 3] = q1.y;
+      }
+    }
+  } else if (full) {
+#pragma unroll (N <= 64 ? EW : 1)
+    for (int w = 0; w < EW; w++)
+#pragma unroll (N <= 64 ? EZ : 1)
+      for (int z = 0; z < EZ; z++)
+#pragma unroll (N <= 64 ? EY : 1)
+        for (int y = 0; y < EY; y++)
+#pragma unroll
+          for (int x = 0; x < EX; x++)
+            raw[x + 4 * y + 16 * z + 64 * w] = __ldg(base + x * s0 + y * s1 + z * s2 + w * s3);
+  } else {
+    for (int w = 0; w < EW; w++)
+      for (int z = 0; z < EZ; z++)
+        for (int y = 0; y < EY; y++)
+#pragma unroll
+          for (int x = 0; x < EX; x++)
+            raw[x + 4 * y + 16 * z + 64 * w] =
+                __ldg(base + pad_index(x, cnt[0]) * s0 + pad_index(y, cnt[1]) * s1 +
+                      pad_index(z, cnt[2]) * s2 + pad_index(w, cnt[3]) * s3);
+  }
+}
+
+template <typename B, int D>
+__device__ __forceinline__ void scatter(const Job& job, uint64_t b, const B (&raw)[1 << (2 * D)]) {
+  constexpr int N = 1 << (2 * D);
+  constexpr int EX = 4, EY = D >= 2 ? 4 : 1, EZ = D >= 3 ? 4 : 1, EW = D >= 4 ? 4 : 1;
+  uint32_t c[4];
+  block_coords(job, b, c);
+  const int64_t s0 = job.s[0], s1 = job.s[1], s2 = job.s[2], s3 = job.s[3];
+  B* base = (B*)job.field + (int64_t)(4 * c[0]) * s0 + (int64_t)(4 * c[1]) * s1 +
+            (int64_t)(4 * c[2]) * s2 + (int64_t)(4 * c[3]) * s3;
+  int cnt[4];
+  bool full = true;
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    const uint32_t left = job.n[a] - 4 * c[a];
+    cnt[a] = a < D ? (left < 4 ? (int)left : 4) : 1;
+    full &= a >= D || cnt[a] == 4;
+  }
+  if (full && (job.flags & kVecOk)) {
+#pragma unroll (N <= 64 ? N / 4 : 1)
+    for (int r = 0; r < N / 4; r++) {
+      const int y = r & 3, z = (r >> 2) & 3, w = r >> 4;
+      B* row = base + y * s1 + z * s2 + w * s3;
+      if constexpr (sizeof(B) == 4) {
+        *(uint4*)row = make_uint4(raw[4 * r + 0], raw[4 * r + 1], raw[4 * r + 2], raw[4 * r + 3]);
+      } else {
+        ((ulonglong2*)row)[0] = make_ulonglong2(raw[4 * r + 0], raw[4 * r + 1]);
+        ((ulonglong2*)row)[1] = make_ulonglong2(raw[4 * r + 2], raw[4 * r + 3]);
+      }
+    }
+  } else if (full) {
+#pragma unroll (N <= 64 ? EW : 1)
+    for (int w = 0; w < EW; w++)
+#pragma unroll (N <= 64 ? EZ : 1)
+      for (int z = 0; z < EZ; z++)
+#pragma unroll (N <= 64 ? EY : 1)
+        for (int y = 0; y < EY; y++)
+#pragma unroll
+          for (int x = 0; x < EX; x++)
+            base[x * s0 + y * s1 + z * s2 + w * s3] = raw[x + 4 * y + 16 * z + 64 * w];
+  } else {
+    for (int w = 0; w < cnt[3]; w++)
+      for (int z = 0; z < cnt[2]; z++)
+        for (int y = 0; y < cnt[1]; y++)
+          for (int x = 0; x < cnt[0]; x++)
+            base[x * s0 + y * s1 + z * s2 + w * s3] = raw[x + 4 * y + 16 * z + 64 * w];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// shared-memory bit sink: a block starts at an arbitrary bit of the tile
+// image; its first and last words may be shared with neighbouring blocks and
+// are combined with atomicOr, every word in between belongs to it alone.
+// The image is zeroed beforehand, so padding only moves the cursor.
+
+struct SmemSink {
+  uint64_t* buf;
+  uint32_t word;
+  unsigned fill;
+  uint64_t acc;
+  bool first;
+
+  __device__ __forceinline__ void store(uint64_t w) {
+    if (first) {
+      atomicOr((unsigned long long*)&buf[word], (unsigned long long)w);
+      first = false;
+    } else {
+      buf[word] = w;
+    }
+    word++;
+  }
+  __device__ __forceinline__ void put(uint64_t v, unsigned n) {
+    if (!n) return;
+    v = low_bits(v, n);
+    acc |= v << fill;
+    const unsigned t = fill + n;
+    if (t >= 64) {
+      store(acc);
+      acc = fill ? v >> (64 - fill) : 0;
+      fill = t - 64;
+    } else {
+      fill = t;
+    }
+  }
+  __device__ __forceinline__ void pad(unsigned n) {
+    const unsigned t = fill + n;
+    if (t >= 64) {
+      store(acc);
+      acc = 0;
+      word += t / 64 - 1;
+      fill = t % 64;
+    } else {
+      fill = t;
+    }
+  }
+  __device__ __forceinline__ void finish() {
+    if (fill) atomicOr((unsigned long long*)&buf[word], (unsigned long long)acc);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// CTA-wide exclusive scan of one value per thread
+
+__device__ __forceinline__ uint32_t cta_exclusive_scan(uint32_t v, uint32_t& total, uint32_t* s_warp) {
+  const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= (unsigned)o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  uint32_t before = 0, sum = 0;
+#pragma unroll
+  for (int w = 0; w < kTile / 32; w++) {
+    const uint32_t t = s_warp[w];
+    before += (unsigned)w < warp ? t : 0;
+    sum += t;
+  }
+  total = sum;
+  return before + x - v;
+}
+
+// ---------------------------------------------------------------------------
+// decoupled look-back (variable-rate streams)
+
+constexpr unsigned long long kStateAgg = 1ull << 62;
+constexpr unsigned long long kStateIncl = 2ull << 62;
+constexpr unsigned long long kStateValue = (1ull << 62) - 1;
+constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at GB300 clocks: then give up
+
+__device__ __forceinline__ void publish_state(unsigned long long* slot, unsigned long long v) {
+  __threadfence();
+  *(volatile unsigned long long*)slot = v;
+}
+
+// Called by all lanes of warp 0.  Returns the number of stream bits taken by
+// the job's tiles before `gt`.
+__device__ __forceinline__ uint64_t look_back(const Job& job, const LaunchScratch& sc, uint32_t gt,
+                                              uint64_t aggregate) {
+  const unsigned lane = threadIdx.x & 31;
+  if (gt == job.tile0) {
+    if (lane == 0) publish_state(sc.tile_state + gt, kStateIncl | aggregate);
+    return 0;
+  }
+  if (lane == 0) publish_state(sc.tile_state + gt, kStateAgg | aggregate);
+  uint64_t exclusive = 0;
+  int64_t pred = (int64_t)gt - 1 - lane;
+  const long long t0 = clock64();
+  bool timed_out = false;
+  for (;;) {
+    unsigned long long st = kStateIncl;  // before the job's first tile: inclusive 0
+    if (pred >= (int64_t)job.tile0) {
+      const volatile unsigned long long* slot = sc.tile_state + pred;
+      st = *slot;
+      while (!(st >> 62)) {
+        if (clock64() - t0 > kWaitCycles) {
+          timed_out = true;
+          st = kStateIncl;
+          break;
+        }
+        __nanosleep(32);
+        st = *slot;
+      }
+    }
+    const unsigned incl = __ballot_sync(0xffffffffu, (st >> 62) == 2);
+    const unsigned limit = incl ? (unsigned)(__ffs(incl) - 1) : 31u;
+    uint64_t part = lane <= limit ? (st & kStateValue) : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    exclusive += part;
+    if (incl) break;
+    pred -= 32;
+  }
+  if (__any_sync(0xffffffffu, timed_out) && lane == 0) atomicOr(&job.result->status, (unsigned)kStatusTimeout);
+  if (lane == 0) publish_state(sc.tile_state + gt, kStateIncl | (exclusive + aggregate));
+  return exclusive;
+}
+
+// ---------------------------------------------------------------------------
+// tile image -> stream words
+
+__device__ __forceinline__ void store_word(const Job& job, uint64_t w, uint64_t v) {
+  if (w < job.cap_words) job.words[w] = v;
+  else atomicOr(&job.result->status, (unsigned)kStatusOverflow);
+}
+
+// a word shared by tiles t-1 (low part) and t (high part): whoever arrives
+// second stores the union
+__device__ __forceinline__ void merge_word(const Job& job, const LaunchScratch& sc, uint32_t t,
+                                           int part, uint64_t w, uint64_t v) {
+  sc.side[2 * (size_t)t + part] = v;
+  __threadfence();
+  if (atomicAdd(&sc.side_cnt[t], 1u) == 1u) {
+    __threadfence();
+    v |= *(volatile unsigned long long*)&sc.side[2 * (size_t)t + (1 - part)];
+    store_word(job, w, v);
+  }
+}
+
+__device__ __forceinline__ void write_tile(const Job& job, const LaunchScratch& sc, uint32_t lt, uint32_t gt,
+                                           const uint64_t* img, uint64_t G, uint32_t total) {
+  const uint64_t E = G + total;
+  const uint64_t hw = G >> 6, tw = E >> 6;
+  const unsigned sh = (unsigned)(G & 63), te = (unsigned)(E & 63);
+  const bool first = lt == 0, last = lt + 1 == job.ntiles;
+  const uint64_t wend = te ? tw + 1 : tw;
+  for (uint64_t w = hw + threadIdx.x; w < wend; w += kTile) {
+    const uint64_t j = w - hw;
+    uint64_t v = sh ? (img[j] << sh) | (j ? img[j - 1] >> (64 - sh) : 0ull) : img[j];
+    if (w == hw && first && sh) v |= job.head_word & ((1ull << sh) - 1);
+    if (w == hw && sh && !first) merge_word(job, sc, gt, 1, w, v);
+    else if (w == tw && te && !last) merge_word(job, sc, gt + 1, 0, w, v);
+    else store_word(job, w, v);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// encode one tile
+
+template <typename S, int D>
+__device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch& sc, uint32_t gt, uint64_t* img) {
+  using B = typename Traits<S>::Bits;
+  constexpr int N = 1 << (2 * D);
+  __shared__ uint32_t s_warp[kTile / 32];
+  __shared__ unsigned long long s_base;
+  const uint32_t lt = gt - job.tile0;
+  const uint64_t b = (uint64_t)lt * kTile + threadIdx.x;
+  const bool active = b < job.nblocks;
+  const bool fixed = job.flags & kFixedRate;
+  const BlockParams p{job.minbits, job.maxbits, job.maxprec, job.minexp};
+
+  BlockCode<S, D> bc;
+  if (active) {
+    B raw[N];
+    gather<B, D>(job, b, raw);
+    prepare_block<S, D>(bc, p, raw);
+  }
+  const uint32_t len = active ? (fixed ? job.maxbits : bc.length()) : 0u;
+  uint32_t total;
+  const uint32_t excl = cta_exclusive_scan(len, total, s_warp);
+
+  const uint32_t nw = (total + 63) / 64 + 1;
+  for (uint32_t i = threadIdx.x; i < nw; i += kTile) img[i] = 0;
+  if (fixed && threadIdx.x == 0) s_base = (unsigned long long)lt * kTile * job.maxbits;
+  __syncthreads();
+
+  if (!fixed && threadIdx.x < 32) {
+    const uint64_t before = look_back(job, sc, gt, total);
+    if (threadIdx.x == 0) s_base = before;
+  }
+  if (active) {
+    SmemSink out{img, excl >> 6, excl & 63u, 0ull, true};
+    bc.emit(out);
+    out.finish();
+  }
+  __syncthreads();
+
+  const uint64_t G = job.bit0 + s_base;
+  write_tile(job, sc, lt, gt, img, G, total);
+  if (active && (job.flags & kWriteIndex)) job.offsets[b] = G + excl;
+  if (threadIdx.x == 0 && lt + 1 == job.ntiles) job.result->end_bit = G + total;
+}
+
+// ---------------------------------------------------------------------------
+// decode one tile
+
+template <typename S, int D>
+__device__ __forceinline__ void decode_tile(const Job& job, uint32_t gt, uint64_t* img, uint32_t img_words) {
+  using B = typename Traits<S>::Bits;
+  constexpr int N = 1 << (2 * D);
+  const uint32_t lt = gt - job.tile0;
+  const uint64_t b0 = (uint64_t)lt * kTile;
+  const uint64_t b = b0 + threadIdx.x;
+  const bool active = b < job.nblocks;
+  const bool fixed = job.flags & kFixedRate;
+  const uint64_t nblk = job.nblocks - b0 < (uint64_t)kTile ? job.nblocks - b0 : (uint64_t)kTile;
+
+  uint64_t Gs, Ge, start = 0, expect = 0;
+  if (fixed) {
+    Gs = job.bit0 + b0 * job.maxbits;
+    Ge = Gs + nblk * job.maxbits;
+    start = Gs + (uint64_t)threadIdx.x * job.maxbits;
+  } else {
+    Gs = job.offsets[b0];
+    Ge = b0 + nblk < job.nblocks ? job.offsets[b0 + nblk] : job.end_bit;
+    if (active) {
+      start = job.offsets[b];
+      expect = b + 1 < job.nblocks ? job.offsets[b + 1] : job.end_bit;
+    }
+  }
+  const uint64_t w0 = Gs >> 6;
+  const uint64_t nwords = Ge >= Gs ? ((Ge + 63) >> 6) - w0 + 2 : ~0ull;
+  const bool staged = nwords <= img_words;
+  if (staged) {
+    for (uint64_t i = threadIdx.x; i < nwords; i += kTile)
+      img[i] = w0 + i < job.cap_words ? __ldg((const unsigned long long*)job.words + w0 + i) : 0ull;
+  }
+  __syncthreads();
+  if (!active) return;
+
+  const BlockParams p{job.minbits, job.maxbits, job.maxprec, job.minexp};
+  B raw[N];
+  uint64_t end;
+  if (staged) {
+    SharedSource in;
+    in.base = img;
+    in.cap = nwords;
+    in.seek(start - (w0 << 6));
+    decode_block<S, D>(in, p, raw);
+    end = in.at + (w0 << 6);
+  } else {
+    WordSource in;
+    in.base = job.words;
+    in.cap = job.cap_words;
+    in.seek(start);
+    decode_block<S, D>(in, p, raw);
+    end = in.at;
+  }
+  if ((job.flags & kVerify) && end != expect) atomicOr(&job.result->status, (unsigned)kStatusIndex);
+  scatter<B, D>(job, b, raw);
+}
+
+// ---------------------------------------------------------------------------
+// kernels.  A launch covers `total_tiles` tiles of one job (passed by value)
+// or of several jobs (device array, sorted by tile0).  With `use_ticket` the
+// CTAs pull tiles from a counter in order; otherwise tile = blockIdx.x.
+
+template <bool kMulti>
+__device__ __forceinline__ const Job* resolve_job(const Job& one, const Job* jobs, int njobs, uint32_t gt, Job* s_job) {
+  if (!kMulti) return &one;
+  if (threadIdx.x == 0) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (jobs[mid].tile0 <= gt) lo = mid;
+      else hi = mid - 1;
+    }
+    *s_job = jobs[lo];
+  }
+  __syncthreads();
+  return s_job;
+}
+
+template <typename S, int D, bool kMulti>
+__global__ void __launch_bounds__(kTile) encode_kernel(const __grid_constant__ Job one, const Job* jobs, int njobs,
+                                                       LaunchScratch sc, uint32_t total_tiles, int use_ticket,
+                                                       uint64_t* gimg, uint32_t img_words) {
+  extern __shared__ uint64_t smem_img[];
+  uint64_t* img = gimg ? gimg + (size_t)blockIdx.x * img_words : smem_img;
+  __shared__ uint32_t s_tile;
+  __shared__ Job s_job;
+  for (uint32_t iter = blockIdx.x;; iter += gridDim.x) {
+    if (threadIdx.x == 0) s_tile = use_ticket ? atomicAdd(sc.ticket, 1u) : iter;
+    __syncthreads();
+    const uint32_t gt = s_tile;
+    if (gt >= total_tiles) break;
+    const Job* job = resolve_job<kMulti>(one, jobs, njobs, gt, &s_job);
+    encode_tile<S, D>(*job, sc, gt, img);
+    __syncthreads();
+  }
+}
+
+template <typename S, int D, bool kMulti>
+__global__ void __launch_bounds__(kTile) decode_kernel(const __grid_constant__ Job one, const Job* jobs, int njobs,
+                                                       uint32_t total_tiles, uint64_t* gimg, uint32_t img_words) {
+  extern __shared__ uint64_t smem_img[];
+  uint64_t* img = gimg ? gimg + (size_t)blockIdx.x * img_words : smem_img;
+  __shared__ Job s_job;
+  for (uint32_t gt = blockIdx.x; gt < total_tiles; gt += gridDim.x) {
+    const Job* job = resolve_job<kMulti>(one, jobs, njobs, gt, &s_job);
+    decode_tile<S, D>(*job, gt, img, img_words);
+    __syncthreads();
+  }
+}
+
+// Recover block offsets of a variable-rate stream that carries no index by
+// walking it block after block (one thread; used only for streams this
+// library did not write).
+template <typename S, int D>
+__global__ void parse_kernel(const __grid_constant__ Job job) {
+  using B = typename Traits<S>::Bits;
+  constexpr int N = 1 << (2 * D);
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const BlockParams p{job.minbits, job.maxbits, job.maxprec, job.minexp};
+  WordSource in;
+  in.base = job.words;
+  in.cap = job.cap_words;
+  in.seek(job.bit0);
+  for (uint64_t b = 0; b < job.nblocks; b++) {
+    job.offsets[b] = in.at;
+    B raw[N];
+    decode_block<S, D>(in, p, raw);
+  }
+  job.result->end_bit = in.at;
+}
+
+}  // namespace zg
