@@ -1,0 +1,448 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 zfp block codec (libzfp_gb300.so) on the
+configuration the reference's headline metric is quoted on: a 3D float32
+512^3 smooth field (seed 1, N(0,1e-2) noise) in four modes -- fixed-rate 8,
+fixed-precision 20, fixed-accuracy 1e-3, reversible -- and the same sweep on
+a 3D float64 384^3 field.
+
+One step = compress then decompress of both fields in all four modes,
+device-resident, through the C ABI (zfp_compress / zfp_decompress,
+zfp_exec_cuda).  value = raw bytes coded per second (both directions).
+e2e = the same sweep with host (pinned) field and stream buffers, so the
+host<->device copies are inside the timed region.  `--impl reference` times
+the reference's CPU algorithm (the oracle port: OpenMP compress, serial
+decompress -- the reference has no OpenMP decompressor) on a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+MODES = [("rate", 8.0), ("precision", 20), ("accuracy", 1e-3), ("reversible", None)]
+FIELDS = [("f32", (512, 512, 512), 1), ("f64", (384, 384, 384), 1)]  # name, shape (z,y,x), seed
+METRIC = "raw GB/s compress+decompress (bit-exact), 3D fp32 512^3 + fp64 384^3, 4 modes"
+SMI_QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--small", action="store_true", help="shrink the fields (smoke runs only)")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def field_shapes(small: bool):
+    if not small:
+        return FIELDS
+    return [("f32", (64, 96, 128), 1), ("f64", (48, 64, 80), 1)]
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+
+class ClockSampler:
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={SMI_QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names[1:], parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """dram bytes per launch of the dominant kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    out = {}
+    try:
+        with open(path) as f:
+            for ln in f:
+                if ln.startswith("#") or ":" not in ln:
+                    continue
+                k, v = ln.split(":", 1)
+                out[k.strip()] = float(v.split()[0])
+    except (OSError, ValueError):
+        pass
+    return out
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+
+class GpuCodec:
+    """Reusable zfp_stream/bitstream/field objects over fixed buffers."""
+
+    def __init__(self, lib, torch, stream_handle):
+        from zfp_gb300 import capi
+        self.lib, self.torch, self.capi = lib, torch, capi
+        self.stream_handle = stream_handle
+
+    def run(self, direction, field_ptr, ztype, n, mode, arg, buf_ptr, buf_bytes, async_=True):
+        lib, capi = self.lib, self.capi
+        bs = lib.stream_open(buf_ptr, buf_bytes)
+        z = lib.zfp_stream_open(bs)
+        capi.set_mode(lib, z, mode, arg, ztype, 3)
+        lib.zfp_stream_set_execution(z, capi.EXEC_CUDA)
+        lib.zfp_gb300_stream_set_cuda_stream(z, self.stream_handle)
+        lib.zfp_gb300_stream_set_async(z, 1 if async_ else 0)
+        f = capi.make_field(lib, field_ptr, ztype, n)
+        r = lib.zfp_compress(z, f) if direction == "c" else lib.zfp_decompress(z, f)
+        lib.zfp_field_free(f)
+        lib.zfp_stream_close(z)
+        lib.stream_close(bs)
+        return r
+
+
+def gpu_arm(args):
+    import torch
+    import torch.distributed as dist
+
+    import zfp_gb300
+    from zfp_gb300 import capi, synth
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = zfp_gb300.load()
+    stream = torch.cuda.current_stream()
+    codec = GpuCodec(lib, torch, stream.cuda_stream)
+
+    fields = []
+    for name, shape, seed in field_shapes(args.small):
+        dt = torch.float32 if name == "f32" else torch.float64
+        x = synth.smooth_field_torch(shape, dt, seed=seed, noise=1e-2)
+        ztype = capi.TYPE_FLOAT if name == "f32" else capi.TYPE_DOUBLE
+        n = tuple(reversed(shape))
+        raw = x.numel() * x.element_size()
+        # worst case stream (reversible) plus a little
+        cap_words = (raw + 4096 * 64) // 8 + x.numel() // 8 + 1024
+        bufs = {m: torch.zeros(cap_words, dtype=torch.int64, device="cuda") for m, _ in MODES}
+        out = torch.empty_like(x)
+        fields.append(dict(name=name, shape=shape, x=x, out=out, ztype=ztype, n=n, raw=raw, bufs=bufs,
+                           cap=cap_words * 8, sizes={}))
+    torch.cuda.synchronize()
+
+    def one(fd, mode, arg, direction):
+        buf = fd["bufs"][mode]
+        ptr = fd["x"].data_ptr() if direction == "c" else fd["out"].data_ptr()
+        r = codec.run(direction, ptr, fd["ztype"], fd["n"], mode, arg, buf.data_ptr(), fd["cap"])
+        if not r:
+            raise RuntimeError(f"{fd['name']} {mode} {direction} failed: {zfp_gb300.last_error()}")
+        if direction == "c":
+            fd["sizes"][mode] = r
+        return r
+
+    def step():
+        for fd in fields:
+            for mode, arg in MODES:
+                one(fd, mode, arg, "c")
+                one(fd, mode, arg, "d")
+
+    # correctness gates on the full fields before timing
+    step()
+    torch.cuda.synchronize()
+    checks = {}
+    for fd in fields:
+        for mode, arg in MODES:
+            one(fd, mode, arg, "c")
+            one(fd, mode, arg, "d")
+            torch.cuda.synchronize()
+            if mode == "reversible":
+                ok = torch.equal(fd["x"].view(torch.int32 if fd["name"] == "f32" else torch.int64),
+                                 fd["out"].view(torch.int32 if fd["name"] == "f32" else torch.int64))
+                checks[f"{fd['name']}_reversible_bitwise"] = bool(ok)
+            elif mode == "accuracy":
+                err = (fd["x"].double() - fd["out"].double()).abs().max().item()
+                checks[f"{fd['name']}_accuracy_maxerr"] = err
+                checks[f"{fd['name']}_accuracy_ok"] = bool(err <= arg)
+            elif mode == "rate":
+                nblocks = np.prod([(s + 3) // 4 for s in fd["shape"]])
+                bits = int(np.floor(64 * arg + 0.5))
+                checks[f"{fd['name']}_rate_size_ok"] = fd["sizes"][mode] == ((nblocks * bits + 63) // 64) * 8
+
+    # per-kernel timing (roofline), each direction/mode alone
+    per = []
+    reps = max(3, args.steps)
+    for fd in fields:
+        for mode, arg in MODES:
+            for direction in ("c", "d"):
+                one(fd, mode, arg, direction)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(reps):
+                    one(fd, mode, arg, direction)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1) / reps
+                comp = fd["sizes"][mode]
+                per.append(dict(field=fd["name"], mode=mode, dir="compress" if direction == "c" else "decompress",
+                                ms=ms, raw_bytes=fd["raw"], stream_bytes=comp,
+                                raw_gbs=fd["raw"] / ms / 1e6, hbm_gbs=(fd["raw"] + comp) / ms / 1e6))
+
+    # timed steps
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms_total = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms_total], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = t.item()
+        dist.barrier()
+    raw_step = sum(2 * fd["raw"] * len(MODES) for fd in fields)
+    value = world * raw_step * args.steps / (ms_total / 1e3) / 1e9
+    launches = 2 * len(MODES) * len(fields) * args.steps
+
+    # roofline of the dominant kernel
+    peak, peak_kind = peak_hbm()
+    dom = max(per, key=lambda r: r["ms"])
+    traffic = ncu_traffic()
+    key = f"{dom['field']}_{dom['mode']}_{dom['dir']}"
+    roofline = {"bound": "hbm", "kernel": key, "achieved": round(dom["hbm_gbs"], 1), "peak": peak,
+                "peak_kind": peak_kind, "unit": "GB/s", "frac": round(dom["hbm_gbs"] / peak, 4),
+                "traffic": traffic.get(key)}
+    fixed = [r for r in per if r["mode"] == "rate"]
+
+    # end to end: host pinned buffers through the same C API (synchronous calls)
+    e2e = None
+    if not args.no_e2e:
+        e2e = e2e_run(lib, torch, codec, fields, args)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(fields, args)
+
+    if rank == 0:
+        clocks = clk.summary()
+        line = {
+            "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_total / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 in, u64 stream", "data": "synthetic",
+            "config": {"workload": "3D float32 512^3 + float64 384^3 smooth fields (8 sinusoids + N(0,1e-2)), "
+                                   "modes rate 8 / precision 20 / accuracy 1e-3 / reversible, compress+decompress, "
+                                   "device-resident", "l2": "inputs larger than L2 (no flush)",
+                       "fields": [list(fd["shape"]) for fd in fields]},
+            "impl": "gb300", "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
+            "gpu_launches": launches,
+            "fixed_rate": {f"{r['field']}_{r['dir']}": {"raw_gbs": round(r["raw_gbs"], 1),
+                                                         "hbm_frac": round(r["hbm_gbs"] / peak, 4)} for r in fixed},
+            "per_kernel": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in r.items()} for r in per],
+            "checks": checks,
+            "compression_ratio": {f"{fd['name']}_{m}": round(fd["raw"] / fd["sizes"][m], 3)
+                                  for fd in fields for m, _ in MODES},
+        }
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def e2e_run(lib, torch, codec, fields, args):
+    """Same sweep, host pinned field and stream buffers: every call uploads
+    its input and downloads its result inside the timed region."""
+    hosts = []
+    for fd in fields:
+        hx = torch.empty(fd["x"].shape, dtype=fd["x"].dtype, pin_memory=True)
+        hx.copy_(fd["x"])
+        hout = torch.empty_like(hx, pin_memory=True)
+        hbuf = torch.zeros(fd["cap"] // 8, dtype=torch.int64, pin_memory=True)
+        hosts.append((fd, hx, hout, hbuf))
+    h2d = d2h = 0
+    sizes = {}
+
+    def step():
+        nonlocal h2d, d2h
+        for fd, hx, hout, hbuf in hosts:
+            for mode, arg in MODES:
+                r = codec.run("c", hx.data_ptr(), fd["ztype"], fd["n"], mode, arg, hbuf.data_ptr(), fd["cap"],
+                              async_=False)
+                r2 = codec.run("d", hout.data_ptr(), fd["ztype"], fd["n"], mode, arg, hbuf.data_ptr(), fd["cap"],
+                               async_=False)
+                if not r or r2 != r:
+                    raise RuntimeError(f"e2e {fd['name']} {mode} failed")
+                sizes[(fd["name"], mode)] = r
+
+    step()
+    torch.cuda.synchronize()
+    n = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(n):
+        step()
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    raw_step = sum(2 * fd["raw"] * len(MODES) for fd in fields)
+    for fd in fields:
+        for mode, _ in MODES:
+            h2d += fd["raw"] + sizes[(fd["name"], mode)]
+            d2h += fd["raw"] + sizes[(fd["name"], mode)]
+    _, world, _ = dist_info()
+    return {"value": round(world * raw_step * n / dt / 1e9, 2), "unit": "GB/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "steps": n, "buffers": "pinned host field and stream"}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle port of the reference's CPU path
+
+def cpu_sample(fields_spec, small):
+    """A bounded sample of each field: the first z-planes (same generator)."""
+    from zfp_gb300 import synth
+    out = []
+    for name, shape, seed in fields_spec:
+        dt = np.float32 if name == "f32" else np.float64
+        planes = max(4, min(shape[0], (48 if name == "f32" else 32) if not small else 8))
+        sub = (planes, shape[1], shape[2])
+        out.append((name, sub, synth.smooth_field(sub, dt, seed=seed, noise=1e-2)))
+    return out
+
+
+def cpu_measure(samples, threads, reps=1):
+    from oracle.pyoracle import Oracle, mode_params
+    orc = Oracle()
+    raw = 0
+    t_c = t_d = 0.0
+    for _ in range(reps):
+        for name, sub, a in samples:
+            for mode, arg in MODES:
+                prm = mode_params(mode, arg, a.dtype, 3)
+                t0 = time.perf_counter()
+                words, end = orc.compress(a, prm, threads=threads)
+                t1 = time.perf_counter()
+                out = np.empty_like(a)
+                orc.decompress(words[: (end + 63) // 64], out, prm)
+                t2 = time.perf_counter()
+                t_c += t1 - t0
+                t_d += t2 - t1
+                raw += 2 * a.nbytes
+    return raw, t_c, t_d
+
+
+def cpu_baseline(fields, args):
+    spec = [(fd["name"], fd["shape"], 1) for fd in fields]
+    samples = cpu_sample(spec, args.small)
+    threads = os.cpu_count() or 1
+    raw, t_c, t_d = cpu_measure(samples, threads)
+    return {"value": round(raw / (t_c + t_d) / 1e9, 4), "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": "oracle (C restatement of the reference's serial codec): OpenMP compress on all cores, "
+                      "serial decompress, over the first z-planes of each field: "
+                      + ", ".join(f"{n} {list(s)}" for n, s, _ in samples),
+            "compress_gbs": round(raw / 2 / t_c / 1e9, 4), "decompress_gbs": round(raw / 2 / t_d / 1e9, 4)}
+
+
+def reference_arm(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    from oracle import pyoracle
+    pyoracle.build()
+    samples = cpu_sample(field_shapes(args.small), args.small)
+    threads = os.cpu_count() or 1
+    cpu_measure(samples, threads)  # warm
+    for _ in range(max(0, args.warmup - 1)):
+        cpu_measure(samples, threads)
+    raw, t_c, t_d = cpu_measure(samples, threads, reps=args.steps)
+    value = raw / (t_c + t_d) / 1e9
+    line = {"metric": METRIC, "value": round(value, 4), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round((t_c + t_d) * 1e3 / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 in, u64 stream",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": "same fields and modes, bounded sample per step (first z-planes)"},
+            "cpu_baseline": {"value": round(value, 4), "unit": "GB/s", "cores": threads, "kind": "port",
+                             "sample": ", ".join(f"{n} {list(s)}" for n, s, _ in samples)},
+            "e2e": {"value": round(value, 4), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,261 @@
+"""GPU codec parity through the C ABI (zfp_compress / zfp_decompress with
+zfp_exec_cuda) against the oracle, bit for bit.
+
+Covers the reference's end-to-end matrix (tests/src/endtoend/zfpEndtoendBase.c:
+1-4D x int32/int64/float/double x fixed rate/precision/accuracy/reversible x
+AS_IS/REVERSED/PERMUTED/INTERLEAVED strides) plus what the GPU path adds:
+host or device field and stream buffers, streams that start mid-word,
+variable-rate streams written elsewhere (no index), and error returns."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle.pyoracle import mode_params
+from zfp_gb300 import capi
+from tests.helpers import geometry, oracle_stream, zfp_run, ztype_of
+
+pytestmark = pytest.mark.gpu
+
+RNG = np.random.default_rng(1234)
+
+MODES = [("rate", 4), ("rate", 8), ("rate", 12.5), ("rate", 1.5), ("precision", 12), ("precision", 24),
+         ("accuracy", 1e-3), ("accuracy", 1e-7), ("reversible", None), ("expert", (100, 300, 20, -30))]
+
+
+def make_values(dtype, shape, kind="smooth"):
+    if np.dtype(dtype).kind == "f":
+        if kind == "special":
+            sp = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 1.0, -2.5, 1e-30, 1e-40, 3e38], dtype=np.float64)
+            if dtype == np.float64:
+                sp = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 1.0, -2.5, 1e-300, 5e-324, 1.7e308])
+            return RNG.choice(sp, size=shape).astype(dtype)
+        x = np.cumsum(RNG.standard_normal(shape), axis=-1)
+        if len(shape) > 1:
+            x = np.cumsum(x, axis=0)
+        return (x * 10.0 ** RNG.uniform(-4, 4)).astype(dtype)
+    bits = 28 if dtype == np.int32 else 58
+    return np.cumsum(RNG.integers(-(1 << 20), 1 << 20, size=shape), axis=-1).clip(-(1 << bits), 1 << bits).astype(dtype)
+
+
+def make_view(base, layout):
+    d = base.ndim
+    if layout == "rev":
+        return base[(slice(None, None, -1),) * d]
+    if layout == "perm" and d >= 2:
+        return np.swapaxes(base, 0, d - 1)
+    if layout == "gap":
+        return base[..., ::2]
+    return base
+
+
+def base_shape(shape, layout):
+    if layout == "gap":
+        return shape[:-1] + (2 * shape[-1],)
+    if layout == "perm" and len(shape) >= 2:
+        s = list(shape)
+        s[0], s[-1] = s[-1], s[0]
+        return tuple(s)
+    return shape
+
+
+class DevSpan:
+    """Device copy of the memory span of a numpy view, addressed like the view."""
+
+    def __init__(self, torch, view, upload=True):
+        n, s = geometry(view)
+        lo = sum(min(0, st * (nn - 1)) for nn, st in zip(n, s))
+        hi = sum(max(0, st * (nn - 1)) for nn, st in zip(n, s))
+        self.isz = view.itemsize
+        self.nbytes = (hi - lo + 1) * self.isz
+        self.host_begin = view.ctypes.data + lo * self.isz
+        self.dev = torch.zeros(self.nbytes, dtype=torch.uint8, device="cuda")
+        if upload:
+            raw = np.ctypeslib.as_array((C.c_uint8 * self.nbytes).from_address(self.host_begin))
+            self.dev.copy_(torch.from_numpy(raw.copy()))
+        self.ptr = self.dev.data_ptr() + (view.ctypes.data - self.host_begin)
+
+    def download_into(self, view):
+        raw = np.ctypeslib.as_array((C.c_uint8 * self.nbytes).from_address(self.host_begin))
+        raw[:] = self.dev.cpu().numpy()
+
+
+def run_case(lib, oracle, torch, dtype, shape, mode, arg, layout="c", field_dev=False, stream_dev=False,
+             prefix=None, kind="smooth", async_=False):
+    base = make_values(dtype, base_shape(shape, layout), kind)
+    view = make_view(base, layout)
+    n, s = geometry(view)
+    zt = ztype_of(view)
+    exp_words, exp_end, prm = oracle_stream(oracle, view, mode, arg, prefix)
+    nwords = len(exp_words) + 16
+
+    fspan = DevSpan(torch, view) if field_dev else None
+    fptr = fspan.ptr if field_dev else view.ctypes.data
+    if stream_dev:
+        sbuf = torch.zeros(nwords, dtype=torch.int64, device="cuda")
+        sptr = sbuf.data_ptr()
+    else:
+        sbuf = np.zeros(nwords, dtype=np.uint64)
+        sptr = sbuf.ctypes.data
+    r, pos = zfp_run(lib, "compress", fptr, zt, n, s, mode, arg, sptr, nwords * 8, prefix, async_=async_)
+    if async_:
+        torch.cuda.synchronize()
+    msg = f"{np.dtype(dtype).name} {shape} {mode}={arg} {layout} fdev={field_dev} sdev={stream_dev} prefix={prefix}"
+    assert r == len(exp_words) * 8, f"size {r} != {len(exp_words) * 8}: {msg}; {lib.zfp_gb300_last_error()}"
+    assert pos == len(exp_words) * 64
+    got = sbuf[: len(exp_words)].cpu().numpy().view(np.uint64) if stream_dev else sbuf[: len(exp_words)]
+    bad = np.nonzero(got != exp_words)[0]
+    assert bad.size == 0, f"stream differs at words {bad[:8]} of {len(exp_words)}: {msg}"
+
+    # decompress into a fresh view of the same layout
+    out_base = np.zeros(base.shape, dtype=dtype)
+    out_view = make_view(out_base, layout)
+    ospan = DevSpan(torch, out_view) if field_dev else None
+    optr = ospan.ptr if field_dev else out_view.ctypes.data
+    r2, pos2 = zfp_run(lib, "decompress", optr, zt, n, s, mode, arg, sptr, nwords * 8, prefix, async_=async_)
+    if async_:
+        torch.cuda.synchronize()
+    assert r2 == len(exp_words) * 8, f"decompress returned {r2}: {msg}; {lib.zfp_gb300_last_error()}"
+    if field_dev:
+        ospan.download_into(out_view)
+    ref_out = np.zeros(view.shape, dtype=dtype)
+    bit0 = 64 * prefix[0] + prefix[2] if prefix else 0
+    oracle.decompress(exp_words, ref_out, prm, bit0)
+    got_out = np.ascontiguousarray(out_view).view(np.uint8)
+    assert np.array_equal(got_out, ref_out.view(np.uint8)), f"decoded values differ: {msg}"
+
+
+SHAPES = {1: [(1,), (7,), (64,), (1001,)], 2: [(1, 1), (5, 7), (16, 16), (37, 61)],
+          3: [(1, 1, 1), (3, 5, 7), (8, 8, 8), (13, 21, 30)], 4: [(2, 3, 5, 6), (4, 4, 4, 4), (5, 9, 7, 6)]}
+DTYPES = [np.float32, np.float64, np.int32, np.int64]
+
+
+@pytest.mark.parametrize("dims", [1, 2, 3, 4])
+@pytest.mark.parametrize("dtype", DTYPES, ids=lambda d: np.dtype(d).name)
+@pytest.mark.parametrize("mode,arg", MODES, ids=lambda v: str(v))
+def test_matrix_host(lib, oracle, cuda, dims, dtype, mode, arg):
+    if mode == "accuracy" and np.dtype(dtype).kind == "i":
+        pytest.skip("accuracy mode is for floating point")
+    for shape in SHAPES[dims]:
+        for layout in ("c", "rev", "perm", "gap"):
+            run_case(lib, oracle, cuda, dtype, shape, mode, arg, layout)
+
+
+@pytest.mark.parametrize("dims", [1, 2, 3, 4])
+@pytest.mark.parametrize("dtype", DTYPES, ids=lambda d: np.dtype(d).name)
+@pytest.mark.parametrize("mode,arg", [("rate", 8), ("precision", 16), ("accuracy", 1e-4), ("reversible", None)],
+                         ids=lambda v: str(v))
+def test_matrix_device(lib, oracle, cuda, dims, dtype, mode, arg):
+    if mode == "accuracy" and np.dtype(dtype).kind == "i":
+        pytest.skip("accuracy mode is for floating point")
+    shape = SHAPES[dims][-1]
+    for layout in ("c", "rev", "perm"):
+        for fdev, sdev in ((True, True), (True, False), (False, True)):
+            run_case(lib, oracle, cuda, dtype, shape, mode, arg, layout, field_dev=fdev, stream_dev=sdev)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=lambda d: np.dtype(d).name)
+@pytest.mark.parametrize("mode,arg", [("rate", 16), ("precision", 30), ("accuracy", 1e-3), ("accuracy", 0.0),
+                                      ("reversible", None)], ids=lambda v: str(v))
+def test_special_values(lib, oracle, cuda, dtype, mode, arg):
+    for dims in (1, 2, 3):
+        run_case(lib, oracle, cuda, dtype, SHAPES[dims][-1], mode, arg, kind="special")
+
+
+@pytest.mark.parametrize("mode,arg", [("rate", 8), ("rate", 5.5), ("accuracy", 1e-3), ("reversible", None)],
+                         ids=lambda v: str(v))
+def test_stream_offsets(lib, oracle, cuda, mode, arg):
+    """Streams that start mid-word, as after zfp_write_header (src/zfp.c:1183)."""
+    for prefix in ((0, 0x5, 3), (2, 0x1234567, 29), (1, (1 << 63) - 5, 63), (3, 0, 0)):
+        run_case(lib, oracle, cuda, np.float32, (9, 10, 11), mode, arg, prefix=prefix)
+        run_case(lib, oracle, cuda, np.float64, (33, 17), mode, arg, prefix=prefix)
+    # device streams: word-aligned start plus bits still held in the stream buffer
+    for prefix in ((1, 0x2b, 7), (0, 0, 0)):
+        run_case(lib, oracle, cuda, np.float32, (9, 10, 11), mode, arg, prefix=prefix, field_dev=True,
+                 stream_dev=True)
+
+
+def test_many_tiles(lib, oracle, cuda):
+    """Fields spanning many CTA tiles: exercises look-back and tile seams."""
+    for mode, arg in (("accuracy", 1e-2), ("precision", 10), ("rate", 3.25), ("reversible", None)):
+        run_case(lib, oracle, cuda, np.float32, (40, 64, 90), mode, arg, field_dev=True, stream_dev=True)
+        run_case(lib, oracle, cuda, np.float64, (40, 64, 90), mode, arg, field_dev=True, stream_dev=True,
+                 prefix=(0, 0x3, 2))
+        run_case(lib, oracle, cuda, np.float32, (257, 129), mode, arg, layout="perm")
+
+
+def test_async_fixed_rate(lib, oracle, cuda):
+    run_case(lib, oracle, cuda, np.float32, (32, 48, 64), "rate", 8, field_dev=True, stream_dev=True, async_=True)
+
+
+def test_foreign_variable_stream(lib, oracle, cuda):
+    """A variable-rate stream this library did not write (no index): the
+    decoder must recover block offsets itself."""
+    torch = cuda
+    for dtype, mode, arg in ((np.float32, "accuracy", 1e-3), (np.float64, "reversible", None),
+                             (np.int32, "precision", 20)):
+        a = make_values(dtype, (19, 23, 17))
+        words, end, prm = oracle_stream(oracle, a, mode, arg)
+        n, s = geometry(a)
+        for sdev in (False, True):
+            if sdev:
+                buf = torch.from_numpy(words.view(np.int64).copy()).cuda()
+                ptr = buf.data_ptr()
+            else:
+                buf = words.copy()
+                ptr = buf.ctypes.data
+            out = np.zeros_like(a)
+            r, _ = zfp_run(lib, "decompress", out.ctypes.data, ztype_of(a), n, s, mode, arg, ptr, words.nbytes)
+            assert r == words.nbytes, lib.zfp_gb300_last_error()
+            ref = np.zeros_like(a)
+            oracle.decompress(words, ref, prm)
+            assert np.array_equal(out.view(np.uint8), ref.view(np.uint8))
+
+
+def test_stale_index_is_detected(lib, oracle, cuda):
+    """Compress field A into a device buffer (the library keeps its block
+    index), overwrite the buffer with a different stream B of the same shape
+    and mode, decompress: the result must be B's, not A's."""
+    torch = cuda
+    a = make_values(np.float32, (16, 24, 20))
+    b = make_values(np.float32, (16, 24, 20)) * 7
+    wb, endb, prm = oracle_stream(oracle, b, "accuracy", 1e-4)
+    n, s = geometry(a)
+    cap = max(len(wb), oracle.max_words(n, np.float32, prm)) + 8
+    buf = torch.zeros(cap, dtype=torch.int64, device="cuda")
+    r, _ = zfp_run(lib, "compress", a.ctypes.data, 3, n, s, "accuracy", 1e-4, buf.data_ptr(), cap * 8)
+    assert r > 0
+    buf.zero_()
+    buf[: len(wb)] = torch.from_numpy(wb.view(np.int64).copy()).cuda()
+    out = np.zeros_like(a)
+    r, _ = zfp_run(lib, "decompress", out.ctypes.data, 3, n, s, "accuracy", 1e-4, buf.data_ptr(), cap * 8)
+    assert r == len(wb) * 8, lib.zfp_gb300_last_error()
+    ref = np.zeros_like(b)
+    oracle.decompress(wb, ref, prm)
+    assert np.array_equal(out, ref)
+
+
+def test_errors_return_zero(lib, cuda):
+    a = make_values(np.float32, (8, 8, 8))
+    n, s = geometry(a)
+    buf = np.zeros(1024, dtype=np.uint64)
+    # serial policy: no CPU codec in this library
+    r, pos = zfp_run(lib, "compress", a.ctypes.data, 3, n, s, "rate", 8, buf.ctypes.data, buf.nbytes,
+                     policy=capi.EXEC_SERIAL)
+    assert r == 0 and pos == 0
+    # OpenMP cannot be selected
+    bs = lib.stream_open(buf.ctypes.data, buf.nbytes)
+    z = lib.zfp_stream_open(bs)
+    assert not lib.zfp_stream_set_execution(z, capi.EXEC_OMP)
+    lib.zfp_stream_close(z)
+    lib.stream_close(bs)
+    # fixed-rate stream that does not fit: refused up front, stream untouched
+    r, pos = zfp_run(lib, "compress", a.ctypes.data, 3, n, s, "rate", 8, buf.ctypes.data, 32 * 8)
+    assert r == 0 and pos == 0
+    # variable-rate overflow detected on the GPU
+    b = make_values(np.float32, (8, 8, 8)) + np.float32(1.0)
+    r, pos = zfp_run(lib, "compress", b.ctypes.data, 3, n, s, "reversible", None, buf.ctypes.data, 16 * 8)
+    assert r == 0 and pos == 0
+    assert "small" in lib.zfp_gb300_last_error().decode()

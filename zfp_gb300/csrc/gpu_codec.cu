@@ -22,6 +22,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/zfp_gb300.h"
@@ -319,31 +320,36 @@ static cudaError_t plan_launch(LaunchArgs& a, uint64_t bound_bits, uint32_t tota
   return cudaSuccess;
 }
 
-static cudaError_t launch_encode_any(int type, int dims, const LaunchArgs& a, cudaStream_t st) {
+template <class F>
+static cudaError_t by_type(int type, int dims, F&& f) {
+  auto d = [&](auto tag) -> cudaError_t {
+    using S = decltype(tag);
+    switch (dims) {
+      case 1: return f(S{}, std::integral_constant<int, 1>{});
+      case 2: return f(S{}, std::integral_constant<int, 2>{});
+      case 3: return f(S{}, std::integral_constant<int, 3>{});
+      case 4: return f(S{}, std::integral_constant<int, 4>{});
+      default: return cudaErrorInvalidValue;
+    }
+  };
   switch (type) {
-    case zfp_type_int32: return launch_encode_i32(dims, a, st);
-    case zfp_type_int64: return launch_encode_i64(dims, a, st);
-    case zfp_type_float: return launch_encode_f32(dims, a, st);
-    default: return launch_encode_f64(dims, a, st);
+    case zfp_type_int32: return d(int32_t{});
+    case zfp_type_int64: return d(int64_t{});
+    case zfp_type_float: return d(float{});
+    default: return d(double{});
   }
+}
+
+static cudaError_t launch_encode_any(int type, int dims, const LaunchArgs& a, cudaStream_t st) {
+  return by_type(type, dims, [&](auto s, auto d) { return run_encode<decltype(s), decltype(d)::value>(a, st); });
 }
 
 static cudaError_t launch_decode_any(int type, int dims, const LaunchArgs& a, cudaStream_t st) {
-  switch (type) {
-    case zfp_type_int32: return launch_decode_i32(dims, a, st);
-    case zfp_type_int64: return launch_decode_i64(dims, a, st);
-    case zfp_type_float: return launch_decode_f32(dims, a, st);
-    default: return launch_decode_f64(dims, a, st);
-  }
+  return by_type(type, dims, [&](auto s, auto d) { return run_decode<decltype(s), decltype(d)::value>(a, st); });
 }
 
 static cudaError_t launch_parse_any(int type, int dims, const Job& j, cudaStream_t st) {
-  switch (type) {
-    case zfp_type_int32: return launch_parse_i32(dims, j, st);
-    case zfp_type_int64: return launch_parse_i64(dims, j, st);
-    case zfp_type_float: return launch_parse_f32(dims, j, st);
-    default: return launch_parse_f64(dims, j, st);
-  }
+  return by_type(type, dims, [&](auto s, auto d) { return run_parse<decltype(s), decltype(d)::value>(j, st); });
 }
 
 // scratch for one launch: result slot + look-back / boundary state, zeroed

@@ -168,8 +168,15 @@ struct SmemSink {
   unsigned fill;
   uint64_t acc;
   bool first;
+  uint32_t cap;       // words in the image; stores past it are dropped and flagged
+  unsigned* status;
 
   __device__ __forceinline__ void store(uint64_t w) {
+    if (word >= cap) {
+      atomicOr(status, (unsigned)kStatusOverflow);
+      word++;
+      return;
+    }
     if (first) {
       atomicOr((unsigned long long*)&buf[word], (unsigned long long)w);
       first = false;
@@ -203,7 +210,9 @@ struct SmemSink {
     }
   }
   __device__ __forceinline__ void finish() {
-    if (fill) atomicOr((unsigned long long*)&buf[word], (unsigned long long)acc);
+    if (!fill) return;
+    if (word < cap) atomicOr((unsigned long long*)&buf[word], (unsigned long long)acc);
+    else atomicOr(status, (unsigned)kStatusOverflow);
   }
 };
 
@@ -309,7 +318,7 @@ __device__ __forceinline__ void merge_word(const Job& job, const LaunchScratch& 
 }
 
 __device__ __forceinline__ void write_tile(const Job& job, const LaunchScratch& sc, uint32_t lt, uint32_t gt,
-                                           const uint64_t* img, uint64_t G, uint32_t total) {
+                                           const uint64_t* img, uint32_t nimg, uint64_t G, uint32_t total) {
   const uint64_t E = G + total;
   const uint64_t hw = G >> 6, tw = E >> 6;
   const unsigned sh = (unsigned)(G & 63), te = (unsigned)(E & 63);
@@ -317,7 +326,9 @@ __device__ __forceinline__ void write_tile(const Job& job, const LaunchScratch& 
   const uint64_t wend = te ? tw + 1 : tw;
   for (uint64_t w = hw + threadIdx.x; w < wend; w += kTile) {
     const uint64_t j = w - hw;
-    uint64_t v = sh ? (img[j] << sh) | (j ? img[j - 1] >> (64 - sh) : 0ull) : img[j];
+    const uint64_t cur = j < nimg ? img[j] : 0ull;
+    const uint64_t prev = j && j - 1 < nimg ? img[j - 1] : 0ull;
+    uint64_t v = sh ? (cur << sh) | (prev >> (64 - sh)) : cur;
     if (w == hw && first && sh) v |= job.head_word & ((1ull << sh) - 1);
     if (w == hw && sh && !first) merge_word(job, sc, gt, 1, w, v);
     else if (w == tw && te && !last) merge_word(job, sc, gt + 1, 0, w, v);
@@ -329,7 +340,8 @@ __device__ __forceinline__ void write_tile(const Job& job, const LaunchScratch& 
 // encode one tile
 
 template <typename S, int D>
-__device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch& sc, uint32_t gt, uint64_t* img) {
+__device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch& sc, uint32_t gt, uint64_t* img,
+                                            uint32_t img_words) {
   using B = typename Traits<S>::Bits;
   constexpr int N = 1 << (2 * D);
   __shared__ uint32_t s_warp[kTile / 32];
@@ -350,7 +362,7 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
   uint32_t total;
   const uint32_t excl = cta_exclusive_scan(len, total, s_warp);
 
-  const uint32_t nw = (total + 63) / 64 + 1;
+  const uint32_t nw = min((total + 63) / 64 + 1, img_words);
   for (uint32_t i = threadIdx.x; i < nw; i += kTile) img[i] = 0;
   if (fixed && threadIdx.x == 0) s_base = (unsigned long long)lt * kTile * job.maxbits;
   __syncthreads();
@@ -360,14 +372,14 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
     if (threadIdx.x == 0) s_base = before;
   }
   if (active) {
-    SmemSink out{img, excl >> 6, excl & 63u, 0ull, true};
+    SmemSink out{img, excl >> 6, excl & 63u, 0ull, true, nw, &job.result->status};
     bc.emit(out);
     out.finish();
   }
   __syncthreads();
 
   const uint64_t G = job.bit0 + s_base;
-  write_tile(job, sc, lt, gt, img, G, total);
+  write_tile(job, sc, lt, gt, img, nw, G, total);
   if (active && (job.flags & kWriteIndex)) job.offsets[b] = G + excl;
   if (threadIdx.x == 0 && lt + 1 == job.ntiles) job.result->end_bit = G + total;
 }
@@ -466,7 +478,7 @@ __global__ void __launch_bounds__(kTile) encode_kernel(const __grid_constant__ J
     const uint32_t gt = s_tile;
     if (gt >= total_tiles) break;
     const Job* job = resolve_job<kMulti>(one, jobs, njobs, gt, &s_job);
-    encode_tile<S, D>(*job, sc, gt, img);
+    encode_tile<S, D>(*job, sc, gt, img, img_words);
     __syncthreads();
   }
 }

@@ -20,23 +20,11 @@ struct LaunchArgs {
   int grid;
 };
 
-// type: zfp_type numbering (1 int32, 2 int64, 3 float, 4 double)
-cudaError_t launch_encode(int type, int dims, const LaunchArgs& a, cudaStream_t st);
-cudaError_t launch_decode(int type, int dims, const LaunchArgs& a, cudaStream_t st);
-cudaError_t launch_parse(int type, int dims, const Job& job, cudaStream_t st);
-
-cudaError_t launch_encode_i32(int dims, const LaunchArgs& a, cudaStream_t st);
-cudaError_t launch_encode_i64(int dims, const LaunchArgs& a, cudaStream_t st);
-cudaError_t launch_encode_f32(int dims, const LaunchArgs& a, cudaStream_t st);
-cudaError_t launch_encode_f64(int dims, const LaunchArgs& a, cudaStream_t st);
-cudaError_t launch_decode_i32(int dims, const LaunchArgs& a, cudaStream_t st);
-cudaError_t launch_decode_i64(int dims, const LaunchArgs& a, cudaStream_t st);
-cudaError_t launch_decode_f32(int dims, const LaunchArgs& a, cudaStream_t st);
-cudaError_t launch_decode_f64(int dims, const LaunchArgs& a, cudaStream_t st);
-cudaError_t launch_parse_i32(int dims, const Job& job, cudaStream_t st);
-cudaError_t launch_parse_i64(int dims, const Job& job, cudaStream_t st);
-cudaError_t launch_parse_f32(int dims, const Job& job, cudaStream_t st);
-cudaError_t launch_parse_f64(int dims, const Job& job, cudaStream_t st);
+// Launchers, one explicit instantiation per (scalar type, dimensionality) in
+// kern_<type>_<dims>d.cu so the 16 variants compile in parallel.
+template <typename S, int D> cudaError_t run_encode(const LaunchArgs& a, cudaStream_t st);
+template <typename S, int D> cudaError_t run_decode(const LaunchArgs& a, cudaStream_t st);
+template <typename S, int D> cudaError_t run_parse(const Job& job, cudaStream_t st);
 
 // largest dynamic shared memory a tile may use before staging moves to global memory
 constexpr size_t kMaxTileSmem = 160 * 1024;

@@ -47,49 +47,17 @@ cudaError_t run_decode(const LaunchArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-template <typename S>
-cudaError_t encode_dims(int dims, const LaunchArgs& a, cudaStream_t st) {
-  switch (dims) {
-    case 1: return run_encode<S, 1>(a, st);
-    case 2: return run_encode<S, 2>(a, st);
-    case 3: return run_encode<S, 3>(a, st);
-    case 4: return run_encode<S, 4>(a, st);
-    default: return cudaErrorInvalidValue;
-  }
-}
-
-template <typename S>
-cudaError_t decode_dims(int dims, const LaunchArgs& a, cudaStream_t st) {
-  switch (dims) {
-    case 1: return run_decode<S, 1>(a, st);
-    case 2: return run_decode<S, 2>(a, st);
-    case 3: return run_decode<S, 3>(a, st);
-    case 4: return run_decode<S, 4>(a, st);
-    default: return cudaErrorInvalidValue;
-  }
-}
-
-template <typename S>
-cudaError_t parse_dims(int dims, const Job& job, cudaStream_t st) {
-  switch (dims) {
-    case 1: parse_kernel<S, 1><<<1, 32, 0, st>>>(job); break;
-    case 2: parse_kernel<S, 2><<<1, 32, 0, st>>>(job); break;
-    case 3: parse_kernel<S, 3><<<1, 32, 0, st>>>(job); break;
-    case 4: parse_kernel<S, 4><<<1, 32, 0, st>>>(job); break;
-    default: return cudaErrorInvalidValue;
-  }
+template <typename S, int D>
+cudaError_t run_parse(const Job& job, cudaStream_t st) {
+  parse_kernel<S, D><<<1, 32, 0, st>>>(job);
   return cudaGetLastError();
 }
 
 }  // namespace zg
 
-#define ZG_DEFINE_LAUNCHERS(SUFFIX, S)                                                        \
-  namespace zg {                                                                              \
-  cudaError_t launch_encode_##SUFFIX(int d, const LaunchArgs& a, cudaStream_t st) {           \
-    return encode_dims<S>(d, a, st);                                                          \
-  }                                                                                           \
-  cudaError_t launch_decode_##SUFFIX(int d, const LaunchArgs& a, cudaStream_t st) {           \
-    return decode_dims<S>(d, a, st);                                                          \
-  }                                                                                           \
-  cudaError_t launch_parse_##SUFFIX(int d, const Job& j, cudaStream_t st) { return parse_dims<S>(d, j, st); } \
+#define ZG_INSTANTIATE(S, D)                                                   \
+  namespace zg {                                                               \
+  template cudaError_t run_encode<S, D>(const LaunchArgs&, cudaStream_t);      \
+  template cudaError_t run_decode<S, D>(const LaunchArgs&, cudaStream_t);      \
+  template cudaError_t run_parse<S, D>(const Job&, cudaStream_t);              \
   }
