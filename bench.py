@@ -47,6 +47,9 @@ def parse_args():
     p.add_argument("--small", action="store_true", help="shrink the fields (smoke runs only)")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--only", default=None,
+                   help="profiling: run one kernel, FIELD:MODE:DIR (e.g. f32:rate:c), --steps times")
+    p.add_argument("--shape", default=None, help="profiling: field shape Z,Y,X for --only")
     return p.parse_args()
 
 
@@ -436,9 +439,42 @@ def reference_arm(args):
     print(json.dumps(line))
 
 
+def profile_one(args):
+    """One kernel on one field, for ncu: field and stream stay on the device."""
+    import torch
+
+    import zfp_gb300
+    from zfp_gb300 import capi, synth
+
+    name, mode, direction = args.only.split(":")
+    arg = dict(MODES)[mode]
+    shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else dict(
+        (f, s) for f, s, _ in FIELDS)[name]
+    torch.cuda.set_device(0)
+    lib = zfp_gb300.load()
+    codec = GpuCodec(lib, torch, torch.cuda.current_stream().cuda_stream)
+    dt = torch.float32 if name == "f32" else torch.float64
+    x = synth.smooth_field_torch(shape, dt, seed=1, noise=1e-2)
+    out = torch.empty_like(x)
+    ztype = capi.TYPE_FLOAT if name == "f32" else capi.TYPE_DOUBLE
+    n = tuple(reversed(shape))
+    cap = x.numel() * x.element_size() * 5 // 4 + (1 << 20)
+    buf = torch.zeros(cap // 8, dtype=torch.int64, device="cuda")
+    size = codec.run("c", x.data_ptr(), ztype, n, mode, arg, buf.data_ptr(), cap, async_=False)
+    assert size, zfp_gb300.last_error()
+    for _ in range(args.steps):
+        ptr = x.data_ptr() if direction == "c" else out.data_ptr()
+        assert codec.run(direction, ptr, ztype, n, mode, arg, buf.data_ptr(), cap, async_=False)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": args.only, "shape": list(shape), "stream_bytes": size,
+                      "raw_bytes": x.numel() * x.element_size()}))
+
+
 def main():
     args = parse_args()
-    if args.impl == "reference":
+    if args.only:
+        profile_one(args)
+    elif args.impl == "reference":
         reference_arm(args)
     else:
         gpu_arm(args)

@@ -89,7 +89,9 @@ class Oracle:
         self.lib.orc_compress.restype = C.c_uint64
         self.lib.orc_compress.argtypes = [pf, pp, pu, C.c_uint64, pu]
         self.lib.orc_compress_par.restype = C.c_uint64
-        self.lib.orc_compress_par.argtypes = [pf, pp, pu, C.c_uint64, C.c_int]
+        self.lib.orc_compress_par.argtypes = [pf, pp, pu, C.c_uint64, C.c_int, pu]
+        self.lib.orc_decompress_par.restype = C.c_uint64
+        self.lib.orc_decompress_par.argtypes = [pf, pp, pu, C.c_uint64, pu, C.c_int]
         self.lib.orc_decompress.restype = C.c_uint64
         self.lib.orc_decompress.argtypes = [pf, pp, pu, C.c_uint64]
         self.lib.orc_blocks.restype = C.c_size_t
@@ -131,7 +133,12 @@ class Oracle:
             words = np.zeros(self.max_words(n, a.dtype, params) + (bit0 >> 6) + 1, dtype=np.uint64)
         wp = words.ctypes.data_as(C.POINTER(C.c_uint64))
         if threads:
-            end = self.lib.orc_compress_par(C.byref(f), C.byref(p), wp, bit0, threads)
+            if block_ends:
+                be = np.zeros(self.lib.orc_blocks(C.byref(f)), dtype=np.uint64)
+                end = self.lib.orc_compress_par(C.byref(f), C.byref(p), wp, bit0, threads,
+                                                be.ctypes.data_as(C.POINTER(C.c_uint64)))
+                return words, int(end), be
+            end = self.lib.orc_compress_par(C.byref(f), C.byref(p), wp, bit0, threads, None)
             return words, int(end)
         if block_ends:
             be = np.zeros(self.lib.orc_blocks(C.byref(f)), dtype=np.uint64)
@@ -140,6 +147,23 @@ class Oracle:
             return words, int(end), be
         end = self.lib.orc_compress(C.byref(f), C.byref(p), wp, bit0, None)
         return words, int(end)
+
+    def decompress_par(self, words: np.ndarray, out: np.ndarray, params, threads: int, block_start=None,
+                       bit0: int = 0, n=None, s=None) -> int:
+        """Parallel decode; block_start = per-block start bits (None: fixed rate)."""
+        if n is None:
+            n, s = self.array_geometry(out)
+        f = self._field(out.ctypes.data, ZTYPE[out.dtype], n, s)
+        p = _Params(*params)
+        w = np.ascontiguousarray(words, dtype=np.uint64)
+        w = np.concatenate([w, np.zeros(2, dtype=np.uint64)])
+        bs = None
+        if block_start is not None:
+            block_start = np.ascontiguousarray(block_start, dtype=np.uint64)
+            bs = block_start.ctypes.data_as(C.POINTER(C.c_uint64))
+        end = self.lib.orc_decompress_par(C.byref(f), C.byref(p), w.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                          bit0, bs, threads)
+        return int(end)
 
     def decompress(self, words: np.ndarray, out: np.ndarray, params, bit0: int = 0, n=None, s=None) -> int:
         if n is None:

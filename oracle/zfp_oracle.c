@@ -433,7 +433,7 @@ unsigned orc_block_maxbits(const orc_field* f, const orc_params* p)
  * private buffer, then copied one after the other into the output.  The
  * output is identical to orc_compress. */
 uint64_t orc_compress_par(const orc_field* f, const orc_params* p,
-                          uint64_t* words, uint64_t bit0, int threads)
+                          uint64_t* words, uint64_t bit0, int threads, uint64_t* block_end)
 {
   geom_t g;
   size_t chunks, c;
@@ -465,6 +465,8 @@ uint64_t orc_compress_par(const orc_field* f, const orc_params* p,
     for (b = b0; b < b1; b++) {
       gather_block(&g, f->data, b, raw);
       encode_one(&w, &g, p, raw);
+      if (block_end)
+        block_end[b] = bw_tell(&w);   /* chunk-relative for now */
     }
     len[c] = bw_tell(&w);
     bw_flush(&w);
@@ -472,6 +474,12 @@ uint64_t orc_compress_par(const orc_field* f, const orc_params* p,
   bw_init(&out, words, bit0);
   for (c = 0; c < chunks; c++) {
     uint64_t i;
+    if (block_end) {
+      size_t b0 = g.blocks * c / chunks, b1 = g.blocks * (c + 1) / chunks, b;
+      uint64_t base = bw_tell(&out);
+      for (b = b0; b < b1; b++)
+        block_end[b] += base;
+    }
     for (i = 0; i < len[c]; i += 64)
       bw_put(&out, buf[c][i >> 6], len[c] - i < 64 ? (unsigned)(len[c] - i) : 64);
     free(buf[c]);
@@ -480,5 +488,34 @@ uint64_t orc_compress_par(const orc_field* f, const orc_params* p,
   free(len);
   end = bw_tell(&out);
   bw_flush(&out);
+  return end;
+}
+
+/* Parallel decompression given every block's start bit (block_start[b]);
+ * with block_start == NULL the stream must be fixed rate (minbits ==
+ * maxbits) and block b starts at bit0 + b * maxbits. */
+uint64_t orc_decompress_par(const orc_field* f, const orc_params* p, const uint64_t* words,
+                            uint64_t bit0, const uint64_t* block_start, int threads)
+{
+  geom_t g;
+  long long b;
+  uint64_t end = bit0;
+  if (!make_geom(f, &g))
+    return bit0;
+  if (threads < 1)
+    threads = 1;
+#ifdef _OPENMP
+  #pragma omp parallel for schedule(static, 256) num_threads(threads) reduction(max : end)
+#endif
+  for (b = 0; b < (long long)g.blocks; b++) {
+    uint64_t raw[256];
+    br_t r;
+    r.words = words;
+    r.pos = block_start ? block_start[b] : bit0 + (uint64_t)b * p->maxbits;
+    decode_one(&r, &g, p, raw);
+    scatter_block(&g, f->data, (size_t)b, raw);
+    if (r.pos > end)
+      end = r.pos;
+  }
   return end;
 }

@@ -58,12 +58,20 @@ uint64_t orc_compress(const orc_field* f, const orc_params* p,
  * into private buffers and concatenated afterwards (the reference's OpenMP
  * driver, src/template/ompcompress.c:155-210 + src/share/parallel.c). */
 uint64_t orc_compress_par(const orc_field* f, const orc_params* p,
-                          uint64_t* words, uint64_t bit0, int threads);
+                          uint64_t* words, uint64_t bit0, int threads, uint64_t* block_end);
 
 /* Decompress from the word buffer starting at bit offset bit0 into the
  * field.  Returns the end bit offset. */
 uint64_t orc_decompress(const orc_field* f, const orc_params* p,
                         const uint64_t* words, uint64_t bit0);
+
+/* Decompress with `threads` OpenMP threads, each block from its start bit
+ * block_start[b] (NULL: fixed rate, block b at bit0 + b * maxbits).  The
+ * reference has no parallel decompressor (src/zfp.c:1137-1138); this one
+ * exists so that full-size fields can be checked quickly.  Returns the
+ * largest block end bit. */
+uint64_t orc_decompress_par(const orc_field* f, const orc_params* p, const uint64_t* words,
+                            uint64_t bit0, const uint64_t* block_start, int threads);
 
 /* Upper bound on the encoded bits of one block for these parameters,
  * the per-block term of zfp_stream_maximum_size (src/zfp.c:712-742). */

@@ -35,7 +35,9 @@ def zfp_run(lib, direction, data_ptr, ztype, n, s, mode, arg, buf_ptr, buf_bytes
             policy=capi.EXEC_CUDA, cuda_stream=None, async_=False):
     """One zfp_compress / zfp_decompress call.  `prefix` = (word, value, nbits)
     positions the stream at bit 64*word + nbits with `value` as the bits
-    already written there.  Returns (return value, stream offset after)."""
+    already written there (for decompression of a device buffer nbits must
+    be 0: a mid-word seek reads the buffer from the host).  Returns
+    (return value, stream offset after)."""
     dims = sum(1 for v in n if v)
     bs = lib.stream_open(buf_ptr, buf_bytes)
     z = lib.zfp_stream_open(bs)

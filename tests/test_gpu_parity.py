@@ -109,7 +109,13 @@ def run_case(lib, oracle, torch, dtype, shape, mode, arg, layout="c", field_dev=
     bad = np.nonzero(got != exp_words)[0]
     assert bad.size == 0, f"stream differs at words {bad[:8]} of {len(exp_words)}: {msg}"
 
-    # decompress into a fresh view of the same layout
+    # decompress into a fresh view of the same layout.  Positioning a stream
+    # mid-word (stream_rseek) reads the buffer from the host, as in the
+    # reference, so a device stream that starts mid-word is read back from a
+    # host copy.
+    if stream_dev and prefix and prefix[2]:
+        hcopy = sbuf.cpu().numpy().view(np.uint64).copy()
+        sptr = hcopy.ctypes.data
     out_base = np.zeros(base.shape, dtype=dtype)
     out_view = make_view(out_base, layout)
     ospan = DevSpan(torch, out_view) if field_dev else None
