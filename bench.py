@@ -47,6 +47,7 @@ def parse_args():
     p.add_argument("--small", action="store_true", help="shrink the fields (smoke runs only)")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-batch", action="store_true")
     p.add_argument("--only", default=None,
                    help="profiling: run one kernel, FIELD:MODE:DIR (e.g. f32:rate:c), --steps times")
     p.add_argument("--shape", default=None, help="profiling: field shape Z,Y,X for --only")
@@ -235,7 +236,7 @@ def gpu_arm(args):
             elif mode == "rate":
                 nblocks = np.prod([(s + 3) // 4 for s in fd["shape"]])
                 bits = int(np.floor(64 * arg + 0.5))
-                checks[f"{fd['name']}_rate_size_ok"] = fd["sizes"][mode] == ((nblocks * bits + 63) // 64) * 8
+                checks[f"{fd['name']}_rate_size_ok"] = bool(fd["sizes"][mode] == ((int(nblocks) * bits + 63) // 64) * 8)
 
     # per-kernel timing (roofline), each direction/mode alone
     per = []
@@ -292,6 +293,8 @@ def gpu_arm(args):
     fixed = [r for r in per if r["mode"] == "rate"]
 
     # end to end: host pinned buffers through the same C API (synchronous calls)
+    ratios = {f"{fd['name']}_{m}": round(fd["raw"] / fd["sizes"][m], 3) for fd in fields for m, _ in MODES}
+    shapes = [list(fd["shape"]) for fd in fields]
     e2e = None
     if not args.no_e2e:
         e2e = e2e_run(lib, torch, codec, fields, args)
@@ -299,6 +302,12 @@ def gpu_arm(args):
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(fields, args)
+
+    batch = None
+    if not args.no_batch:
+        del fields
+        torch.cuda.empty_cache()
+        batch = batch_compare(lib, torch, stream, args)
 
     if rank == 0:
         clocks = clk.summary()
@@ -309,19 +318,131 @@ def gpu_arm(args):
             "config": {"workload": "3D float32 512^3 + float64 384^3 smooth fields (8 sinusoids + N(0,1e-2)), "
                                    "modes rate 8 / precision 20 / accuracy 1e-3 / reversible, compress+decompress, "
                                    "device-resident", "l2": "inputs larger than L2 (no flush)",
-                       "fields": [list(fd["shape"]) for fd in fields]},
+                       "fields": shapes},
             "impl": "gb300", "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
             "gpu_launches": launches,
             "fixed_rate": {f"{r['field']}_{r['dir']}": {"raw_gbs": round(r["raw_gbs"], 1),
                                                          "hbm_frac": round(r["hbm_gbs"] / peak, 4)} for r in fixed},
             "per_kernel": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in r.items()} for r in per],
             "checks": checks,
-            "compression_ratio": {f"{fd['name']}_{m}": round(fd["raw"] / fd["sizes"][m], 3)
-                                  for fd in fields for m, _ in MODES},
+            "compression_ratio": ratios,
+            "batch": batch,
         }
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
+
+
+def bind_batch(lib):
+    from zfp_gb300 import capi
+    L = lib.lib
+    L.zfp_gb300_batch_create.restype = C.c_void_p
+    L.zfp_gb300_batch_create.argtypes = [C.POINTER(capi.PZ), C.POINTER(capi.PF), C.c_size_t, C.c_int]
+    L.zfp_gb300_batch_run.restype = C.c_int
+    L.zfp_gb300_batch_run.argtypes = [C.c_void_p, C.c_void_p]
+    L.zfp_gb300_batch_finish.restype = C.c_int
+    L.zfp_gb300_batch_finish.argtypes = [C.c_void_p, C.POINTER(C.c_size_t)]
+    L.zfp_gb300_batch_free.argtypes = [C.c_void_p]
+    return L
+
+
+def batch_compare(lib, torch, stream, args):
+    """4096 independent 3D float32 arrays, extents log-uniform in [8,128]
+    (seed 2), amplitude scale 10^U(-3,3); half fixed-rate (rate in
+    {4,8,12,16,24,32}), half fixed-accuracy (tolerance 10^U(-5,-2)).  One
+    batched launch against one zfp_compress / zfp_decompress per array."""
+    from zfp_gb300 import capi, synth
+    L = bind_batch(lib)
+    rng = np.random.default_rng(2)
+    count = 4096 if not args.small else 256
+    arrays = []
+    for i in range(count):
+        shape = tuple(int(v) for v in np.exp(rng.uniform(np.log(8), np.log(128), size=3)).astype(int))
+        scale = float(10.0 ** rng.uniform(-3, 3))
+        x = synth.smooth_field_torch(shape, torch.float32, seed=int(rng.integers(1 << 31)), noise=1e-2, scale=scale)
+        if i % 2 == 0:
+            mode, arg = "rate", float(rng.choice([4, 8, 12, 16, 24, 32]))
+        else:
+            mode, arg = "accuracy", float(10.0 ** rng.uniform(-5, -2))
+        arrays.append((x, mode, arg))
+    raw = sum(x.numel() * 4 for x, _, _ in arrays)
+
+    def objects(outs, bufs, use_out):
+        zs, fs, keep = [], [], []
+        for (x, mode, arg), o, buf in zip(arrays, outs, bufs):
+            bs = lib.stream_open(buf.data_ptr(), buf.numel() * 8)
+            z = lib.zfp_stream_open(bs)
+            capi.set_mode(lib, z, mode, arg, capi.TYPE_FLOAT, 3)
+            lib.zfp_stream_set_execution(z, capi.EXEC_CUDA)
+            lib.zfp_gb300_stream_set_cuda_stream(z, stream.cuda_stream)
+            lib.zfp_gb300_stream_set_async(z, 1)
+            f = capi.make_field(lib, (o if use_out else x).data_ptr(), capi.TYPE_FLOAT, tuple(reversed(x.shape)))
+            zs.append(z)
+            fs.append(f)
+            keep.append(bs)
+        return zs, fs, keep
+
+    def close(zs, fs, keep):
+        for z, f, bs in zip(zs, fs, keep):
+            lib.zfp_field_free(f)
+            lib.zfp_stream_close(z)
+            lib.stream_close(bs)
+
+    def buffers():
+        out = []
+        for x, mode, arg in arrays:
+            z = lib.zfp_stream_open(None)
+            capi.set_mode(lib, z, mode, arg, capi.TYPE_FLOAT, 3)
+            f = capi.make_field(lib, 0, capi.TYPE_FLOAT, tuple(reversed(x.shape)))
+            nbytes = lib.zfp_stream_maximum_size(z, f)
+            lib.zfp_field_free(f)
+            lib.zfp_stream_close(z)
+            out.append(torch.zeros(nbytes // 8 + 8, dtype=torch.int64, device="cuda"))
+        return out
+
+    per_bufs, bat_bufs = buffers(), buffers()
+    per_out = [torch.empty_like(x) for x, _, _ in arrays]
+    bat_out = [torch.empty_like(x) for x, _, _ in arrays]
+    reps = max(2, min(args.steps, 5))
+    result = {"arrays": count, "raw_bytes": raw}
+    for direction, name in ((0, "compress"), (1, "decompress")):
+        # one launch per array
+        zs, fs, keep = objects(per_out, per_bufs, direction == 1)
+        fn = lib.zfp_compress if direction == 0 else lib.zfp_decompress
+        for z, f in zip(zs, fs):       # warm-up (and, for decompress, index lookups)
+            lib.zfp_stream_rewind(z)
+            assert fn(z, f)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            for z, f in zip(zs, fs):
+                lib.zfp_stream_rewind(z)
+                fn(z, f)
+        torch.cuda.synchronize()
+        per_s = (time.perf_counter() - t0) / reps
+        close(zs, fs, keep)
+        # one batched launch
+        zs, fs, keep = objects(bat_out, bat_bufs, direction == 1)
+        b = L.zfp_gb300_batch_create((capi.PZ * count)(*zs), (capi.PF * count)(*fs), count, direction)
+        assert b, lib.zfp_gb300_last_error()
+        sizes = (C.c_size_t * count)()
+        assert L.zfp_gb300_batch_run(b, stream.cuda_stream)   # autotune + graph capture
+        assert L.zfp_gb300_batch_finish(b, sizes)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            L.zfp_gb300_batch_run(b, stream.cuda_stream)
+        torch.cuda.synchronize()
+        bat_s = (time.perf_counter() - t0) / reps
+        assert L.zfp_gb300_batch_finish(b, sizes)
+        L.zfp_gb300_batch_free(b)
+        close(zs, fs, keep)
+        same = all(torch.equal(p, q) for p, q in zip(per_bufs, bat_bufs)) if direction == 0 else \
+            all(torch.equal(p.view(torch.int32), q.view(torch.int32)) for p, q in zip(per_out, bat_out))
+        result[name] = {"per_array_gbs": round(raw / per_s / 1e9, 2), "batched_gbs": round(raw / bat_s / 1e9, 2),
+                        "speedup": round(per_s / bat_s, 2), "bit_identical": bool(same),
+                        "per_array_ms": round(per_s * 1e3, 3), "batched_ms": round(bat_s * 1e3, 3)}
+    return result
 
 
 def e2e_run(lib, torch, codec, fields, args):

@@ -33,6 +33,37 @@ zfp_bool zfp_gb300_stream_synchronize(zfp_stream* zfp);
 /* Reason for the last failure (return value 0) seen by this thread, or "". */
 const char* zfp_gb300_last_error(void);
 
+/* ---- batches: many fields in one launch --------------------------------
+ * A batch codes `count` independent fields, each with its own zfp_stream
+ * (mode, parameters and bit stream, positioned where that stream's next
+ * zfp_compress / zfp_decompress would start).  Field data and stream
+ * buffers must be device memory.  Fields of the same scalar type and
+ * dimensionality run as one persistent launch whose CTAs pull tiles of
+ * blocks from a shared counter, so thousands of small, uneven fields keep
+ * every SM busy; the launches are captured in a CUDA graph on the first run
+ * and replayed afterwards.  The streams, fields and their buffers must stay
+ * valid and unchanged in shape until the batch is freed. */
+typedef struct zfp_gb300_batch zfp_gb300_batch;
+
+/* direction: 0 = compress, 1 = decompress.  NULL on failure. */
+zfp_gb300_batch* zfp_gb300_batch_create(zfp_stream* const* streams, const zfp_field* const* fields,
+                                        size_t count, int direction);
+
+/* Queue the batch on `cuda_stream` (NULL = legacy default stream); returns
+ * without waiting. */
+zfp_bool zfp_gb300_batch_run(zfp_gb300_batch* batch, void* cuda_stream);
+
+/* Wait for the last run, leave every bit stream as zfp_compress /
+ * zfp_decompress would and store each field's stream size in bytes in
+ * sizes[i] (0 if that field failed).  Returns zfp_false if any failed. */
+zfp_bool zfp_gb300_batch_finish(zfp_gb300_batch* batch, size_t* sizes);
+
+void zfp_gb300_batch_free(zfp_gb300_batch* batch);
+
+/* CTAs per SM of the persistent batch launch; 0 (default) picks the value
+ * the built-in autotuner measured fastest for this batch on its first run. */
+zfp_bool zfp_gb300_batch_set_ctas_per_sm(zfp_gb300_batch* batch, int ctas_per_sm);
+
 #ifdef __cplusplus
 }
 #endif

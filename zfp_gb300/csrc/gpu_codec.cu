@@ -29,6 +29,7 @@
 #include "job.h"
 #include "launch.h"
 #include "runtime.h"
+#include "gpu_internal.h"
 
 namespace zg {
 
@@ -39,23 +40,17 @@ static thread_local std::string g_last_error;
 
 void set_error(const char* msg) { g_last_error = msg ? msg : ""; }
 
-static size_t fail(const char* msg) {
+size_t fail(const char* msg) {
   set_error(msg);
   return 0;
 }
 
-static size_t fail_cuda(const char* where, cudaError_t e) {
+size_t fail_cuda(const char* where, cudaError_t e) {
   std::string m = std::string(where) + ": " + cudaGetErrorString(e);
   set_error(m.c_str());
   return 0;
 }
 
-struct ExecParams {
-  uint32_t magic;
-  cudaStream_t stream;
-  int async;
-};
-static const uint32_t kExecMagic = 0x7a673330u;  // identifies params owned by this library
 
 bool ensure_exec_params(zfp_stream* z) {
   if (z->exec.policy == zfp_exec_cuda && z->exec.params) return true;
@@ -74,7 +69,7 @@ void release_exec_params(zfp_stream* z) {
   z->exec.params = nullptr;
 }
 
-static ExecParams* exec_params(zfp_stream* z) {
+ExecParams* exec_params(zfp_stream* z) {
   ExecParams* p = (ExecParams*)z->exec.params;
   return (p && p->magic == kExecMagic) ? p : nullptr;
 }
@@ -82,7 +77,7 @@ static ExecParams* exec_params(zfp_stream* z) {
 // ---------------------------------------------------------------------------
 // memory
 
-static bool is_device_ptr(const void* p) {
+bool is_device_ptr(const void* p) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
@@ -91,7 +86,7 @@ static bool is_device_ptr(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-static void init_pool_once() {
+void init_pool_once() {
   static std::once_flag flag;
   std::call_once(flag, [] {
     int dev = 0;
@@ -104,34 +99,12 @@ static void init_pool_once() {
   });
 }
 
-// stream-ordered device buffer
-struct DevBuf {
-  void* p = nullptr;
-  cudaStream_t st = nullptr;
-  cudaError_t alloc(size_t bytes, cudaStream_t s) {
-    st = s;
-    return cudaMallocAsync(&p, bytes ? bytes : 8, s);
-  }
-  void release() {
-    if (p) cudaFreeAsync(p, st);
-    p = nullptr;
-  }
-  ~DevBuf() { release(); }
-};
 
 // ---------------------------------------------------------------------------
 // field description
 
-struct FieldInfo {
-  int type = 0, dims = 0;
-  size_t esize = 0;
-  uint32_t n[4] = {1, 1, 1, 1}, nb[4] = {1, 1, 1, 1};
-  int64_t s[4] = {0, 0, 0, 0};
-  uint64_t nblocks = 0;
-  ptrdiff_t lo = 0, hi = 0;  // lowest / highest element offset
-};
 
-static const char* field_info(const zfp_field* f, FieldInfo& fi) {
+const char* field_info(const zfp_field* f, FieldInfo& fi) {
   switch (f->type) {
     case zfp_type_int32: case zfp_type_float: fi.esize = 4; break;
     case zfp_type_int64: case zfp_type_double: fi.esize = 8; break;
@@ -162,7 +135,7 @@ static const char* field_info(const zfp_field* f, FieldInfo& fi) {
 }
 
 // header bits a block can carry before its bit planes
-static uint32_t header_max(int type, bool rev) {
+uint32_t header_max(int type, bool rev) {
   switch (type) {
     case zfp_type_int32: return rev ? 5 : 0;
     case zfp_type_int64: return rev ? 6 : 0;
@@ -174,7 +147,7 @@ static uint32_t header_max(int type, bool rev) {
 // upper bound on the bits of one block (the block term of
 // zfp_stream_maximum_size, src/zfp.c:712-742, widened where a maxbits
 // below the header size makes the reference's budget wrap around)
-static uint64_t block_bound(const FieldInfo& fi, const zfp_stream* z) {
+uint64_t block_bound(const FieldInfo& fi, const zfp_stream* z) {
   const bool rev = z->minexp < ZFP_MIN_EXP;
   const uint64_t values = 1ull << (2 * fi.dims);
   const uint64_t prec = 8 * fi.esize;
@@ -185,12 +158,12 @@ static uint64_t block_bound(const FieldInfo& fi, const zfp_stream* z) {
   return std::max<uint64_t>(b, z->minbits);
 }
 
-static bool is_fixed_rate(const FieldInfo& fi, const zfp_stream* z) {
+bool is_fixed_rate(const FieldInfo& fi, const zfp_stream* z) {
   const bool rev = z->minexp < ZFP_MIN_EXP;
   return !rev && z->minbits == z->maxbits && z->maxbits >= header_max(fi.type, false) && z->maxbits > 0;
 }
 
-static bool vector_ok(const FieldInfo& fi, const void* data) {
+bool vector_ok(const FieldInfo& fi, const void* data) {
   if (fi.s[0] != 1 || ((uintptr_t)data & 15)) return false;
   for (int a = 1; a < fi.dims; a++)
     if ((fi.s[a] * (int64_t)fi.esize) % 16) return false;
@@ -200,16 +173,6 @@ static bool vector_ok(const FieldInfo& fi, const void* data) {
 // ---------------------------------------------------------------------------
 // index registry for variable-rate streams
 
-struct IndexEntry {
-  const void* begin;
-  uint64_t bit0, end_bit, nblocks;
-  int type, dims;
-  uint32_t minbits, maxbits, maxprec;
-  int32_t minexp;
-  uint64_t* offsets;       // device, nblocks words
-  cudaStream_t stream;     // last stream that used it (frees are ordered after it)
-  uint64_t tick;
-};
 
 static std::mutex g_reg_mu;
 static std::vector<IndexEntry> g_reg;
@@ -227,7 +190,7 @@ static void free_entry(IndexEntry& e) {
 }
 
 // drop entries of the same buffer whose stream range overlaps [bit0, end)
-static void registry_invalidate(const void* begin, uint64_t bit0, uint64_t end) {
+void registry_invalidate(const void* begin, uint64_t bit0, uint64_t end) {
   std::lock_guard<std::mutex> lk(g_reg_mu);
   for (size_t i = 0; i < g_reg.size();) {
     IndexEntry& e = g_reg[i];
@@ -240,7 +203,7 @@ static void registry_invalidate(const void* begin, uint64_t bit0, uint64_t end) 
   }
 }
 
-static void registry_insert(const IndexEntry& ne) {
+void registry_insert(const IndexEntry& ne) {
   registry_invalidate(ne.begin, ne.bit0, ne.end_bit);
   std::lock_guard<std::mutex> lk(g_reg_mu);
   size_t bytes = ne.nblocks * 8;
@@ -256,7 +219,7 @@ static void registry_insert(const IndexEntry& ne) {
   g_reg.back().tick = ++g_tick;
 }
 
-static bool registry_find(const void* begin, uint64_t bit0, const FieldInfo& fi, const zfp_stream* z,
+bool registry_find(const void* begin, uint64_t bit0, const FieldInfo& fi, const zfp_stream* z,
                           cudaStream_t st, IndexEntry& out) {
   std::lock_guard<std::mutex> lk(g_reg_mu);
   for (auto& e : g_reg)
@@ -274,7 +237,7 @@ static bool registry_find(const void* begin, uint64_t bit0, const FieldInfo& fi,
 // ---------------------------------------------------------------------------
 // launch helpers
 
-static Job base_job(const FieldInfo& fi, const zfp_stream* z, void* field) {
+Job base_job(const FieldInfo& fi, const zfp_stream* z, void* field) {
   Job j;
   std::memset(&j, 0, sizeof j);
   j.field = field;
@@ -293,7 +256,7 @@ static Job base_job(const FieldInfo& fi, const zfp_stream* z, void* field) {
   return j;
 }
 
-static int persistent_grid() {
+int persistent_grid() {
   static int sms = [] {
     int dev = 0, n = 0;
     cudaGetDevice(&dev);
@@ -340,15 +303,15 @@ static cudaError_t by_type(int type, int dims, F&& f) {
   }
 }
 
-static cudaError_t launch_encode_any(int type, int dims, const LaunchArgs& a, cudaStream_t st) {
+cudaError_t launch_encode_any(int type, int dims, const LaunchArgs& a, cudaStream_t st) {
   return by_type(type, dims, [&](auto s, auto d) { return run_encode<decltype(s), decltype(d)::value>(a, st); });
 }
 
-static cudaError_t launch_decode_any(int type, int dims, const LaunchArgs& a, cudaStream_t st) {
+cudaError_t launch_decode_any(int type, int dims, const LaunchArgs& a, cudaStream_t st) {
   return by_type(type, dims, [&](auto s, auto d) { return run_decode<decltype(s), decltype(d)::value>(a, st); });
 }
 
-static cudaError_t launch_parse_any(int type, int dims, const Job& j, cudaStream_t st) {
+cudaError_t launch_parse_any(int type, int dims, const Job& j, cudaStream_t st) {
   return by_type(type, dims, [&](auto s, auto d) { return run_parse<decltype(s), decltype(d)::value>(j, st); });
 }
 

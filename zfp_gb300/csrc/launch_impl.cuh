@@ -16,7 +16,7 @@ static void allow_smem(K kernel) {
 template <typename S, int D>
 cudaError_t run_encode(const LaunchArgs& a, cudaStream_t st) {
   const size_t smem = a.gimg ? 0 : (size_t)a.img_words * 8;
-  if (a.njobs > 1) {
+  if (a.jobs) {  // device job array: the multi-job kernel
     static const bool once = (allow_smem(encode_kernel<S, D, true>), true);
     (void)once;
     encode_kernel<S, D, true><<<a.grid, kTile, smem, st>>>(a.one, a.jobs, a.njobs, a.sc, a.total_tiles,
@@ -33,7 +33,7 @@ cudaError_t run_encode(const LaunchArgs& a, cudaStream_t st) {
 template <typename S, int D>
 cudaError_t run_decode(const LaunchArgs& a, cudaStream_t st) {
   const size_t smem = a.gimg ? 0 : (size_t)a.img_words * 8;
-  if (a.njobs > 1) {
+  if (a.jobs) {  // device job array: the multi-job kernel
     static const bool once = (allow_smem(decode_kernel<S, D, true>), true);
     (void)once;
     decode_kernel<S, D, true><<<a.grid, kTile, smem, st>>>(a.one, a.jobs, a.njobs, a.total_tiles, a.gimg,
