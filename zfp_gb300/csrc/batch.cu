@@ -246,7 +246,8 @@ zfp_gb300_batch* zfp_gb300_batch_create(zfp_stream* const* streams, const zfp_fi
     g.sc.tile_state = (unsigned long long*)(p + 64);
     g.sc.side = (unsigned long long*)(p + 64 + t * 8);
     g.sc.side_cnt = (unsigned int*)(p + 64 + t * 24);
-    if ((size_t)g.img_words * 8 > kMaxTileSmem) {
+    const size_t extra = b->direction == 0 ? plane_bytes(b->info[g.members[0]].esize, g.dims) : 0;
+    if ((size_t)g.img_words * 8 + extra > kMaxTileSmem) {
       g.gimg_words = (size_t)persistent_grid() * 2 * g.img_words;
       if ((e = cudaMalloc((void**)&g.gimg, g.gimg_words * 8)) != cudaSuccess) {
         fail_cuda("zfp_gb300_batch_create: staging", e);

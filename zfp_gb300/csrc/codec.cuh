@@ -90,6 +90,23 @@ ZG_HD uint32_t byte_perm(uint32_t x, uint32_t y, uint32_t s) {
 
 ZG_HD uint64_t low_bits(uint64_t v, unsigned n) { return n >= 64 ? v : v & ((uint64_t(1) << n) - 1); }
 
+ZG_HD int popc64(uint64_t x) {
+#if defined(__CUDA_ARCH__)
+  return __popcll(x);
+#else
+  return __builtin_popcountll(x);
+#endif
+}
+
+// count of leading zeros of a nonzero word
+ZG_HD int clz64(uint64_t x) {
+#if defined(__CUDA_ARCH__)
+  return __clzll((long long)x);
+#else
+  return __builtin_clzll(x);
+#endif
+}
+
 // ---------------------------------------------------------------------------
 // coefficient order (src/template/codec{2,3,4}.c): by total sequency
 // i+j+k(+l), then by i^2+j^2+k^2(+l^2); ties in the order the format fixes.
@@ -734,35 +751,15 @@ struct CountSink {
   ZG_HD void pad(unsigned k) { n += k; }
 };
 
-template <typename S, int D>
-struct BlockCode {
-  using U = typename Traits<S>::UInt;
-  static constexpr int N = 1 << (2 * D);
-  static constexpr int P = 8 * sizeof(U);
-  static constexpr bool kWide = N > 64;
+// Everything about a block except its bit planes: header bits, the budget
+// left for the plane coder, the planes to code and the minimum size.
+struct BlockHead {
   uint64_t hdr;        // header bits, first bit in the LSB
   unsigned hdr_bits;
   unsigned budget;     // bits granted to the plane coder (unsigned wrap as in the reference)
   unsigned maxprec;    // bit planes to code
   unsigned pad_to;     // the block is padded with zeros to at least this many bits
   bool coded;          // false: header only
-  typename std::conditional<kWide, U[N], uint64_t[P]>::type data;  // planes, or coefficients for 4D
-
-  template <class Sink>
-  ZG_HD unsigned emit(Sink& out) const {
-    out.put(hdr, hdr_bits);
-    unsigned bits = hdr_bits;
-    if (coded) {
-      if constexpr (kWide) bits += encode_planes_wide<U>(out, budget, maxprec, data);
-      else bits += encode_planes<P, N>(out, budget, maxprec, data);
-    }
-    if (bits < pad_to) { out.pad(pad_to - bits); bits = pad_to; }
-    return bits;
-  }
-  ZG_HD unsigned length() const {
-    CountSink c;
-    return emit(c);
-  }
 };
 
 // reorder by sequency and map to negabinary (src/template/encode.c:83-88)
@@ -771,16 +768,6 @@ ZG_HD void reorder(const I (&v)[1 << (2 * D)], typename std::make_unsigned<I>::t
   constexpr int N = 1 << (2 * D);
 #pragma unroll (N <= 64 ? N : 1)
   for (int i = 0; i < N; i++) u[i] = to_nb<I>(v[perm<D>(i)]);
-}
-
-template <typename S, int D>
-ZG_HD void set_coeffs(BlockCode<S, D>& bc, const typename Traits<S>::UInt (&u)[1 << (2 * D)]) {
-  constexpr int N = 1 << (2 * D);
-  if constexpr (BlockCode<S, D>::kWide) {
-    for (int i = 0; i < N; i++) bc.data[i] = u[i];
-  } else {
-    make_planes<N>(u, bc.data);
-  }
 }
 
 // precision of a reversible block: top plane down to the lowest set bit of
@@ -796,12 +783,14 @@ ZG_HD unsigned rev_precision(const U (&u)[N], unsigned maxprec) {
   return prec;
 }
 
-// Prepare one gathered block of scalar type S (bit patterns in `raw`).
-// Lossy floating point: src/template/encodef.c:63-90; reversible floating
-// point: revencodef.c:45-80; integers: encode.c:260-280, revencode.c:57-79.
+// Front end of one gathered block of scalar type S (bit patterns in `raw`):
+// fills the head and, for coded blocks, the reordered negabinary
+// coefficients.  Lossy floating point: src/template/encodef.c:63-90;
+// reversible floating point: revencodef.c:45-80; integers: encode.c:260-280,
+// revencode.c:57-79.
 template <typename S, int D>
-ZG_HD void prepare_block(BlockCode<S, D>& bc, const BlockParams& p,
-                         const typename Traits<S>::Bits (&raw)[1 << (2 * D)]) {
+ZG_HD void prepare_coeffs(BlockHead& h, const BlockParams& p, const typename Traits<S>::Bits (&raw)[1 << (2 * D)],
+                          typename Traits<S>::UInt (&u)[1 << (2 * D)]) {
   using T = Traits<S>;
   using B = typename T::Bits;
   using I = typename T::Int;
@@ -809,9 +798,8 @@ ZG_HD void prepare_block(BlockCode<S, D>& bc, const BlockParams& p,
   constexpr int N = 1 << (2 * D);
   const bool rev = p.minexp < kMinExp;
   I v[N];
-  U u[N];
-  bc.pad_to = p.minbits;
-  bc.coded = true;
+  h.pad_to = p.minbits;
+  h.coded = true;
   if constexpr (T::kFloat) {
     bool special;
     const int emax = block_emax<S, N>(raw, special);
@@ -819,17 +807,16 @@ ZG_HD void prepare_block(BlockCode<S, D>& bc, const BlockParams& p,
       const unsigned maxprec = coded_precision(emax, p.maxprec, p.minexp, D);
       const unsigned e = maxprec ? (unsigned)(emax + T::kEBias) : 0u;
       if (!e) {                                    // single zero bit, padded to minbits
-        bc.hdr = 0; bc.hdr_bits = 1; bc.coded = false;
+        h.hdr = 0; h.hdr_bits = 1; h.coded = false;
         return;
       }
-      bc.hdr = 2 * (uint64_t)e + 1;
-      bc.hdr_bits = 1 + T::kEBits;
-      bc.budget = p.maxbits - bc.hdr_bits;
-      bc.maxprec = maxprec;
+      h.hdr = 2 * (uint64_t)e + 1;
+      h.hdr_bits = 1 + T::kEBits;
+      h.budget = p.maxbits - h.hdr_bits;
+      h.maxprec = maxprec;
       fwd_cast<S, N>(raw, v, emax, special);
       xform<kFwd, D>(v);
       reorder<D>(v, u);
-      set_coeffs(bc, u);
       return;
     }
     constexpr B kTc = ~(B(1) << (8 * sizeof(B) - 1));
@@ -847,53 +834,208 @@ ZG_HD void prepare_block(BlockCode<S, D>& bc, const BlockParams& p,
     if (exact) {
       const unsigned e = (unsigned)(emax + T::kEBias);
       if (!e) {                                    // all-zero block: one bit, never padded
-        bc.hdr = 0; bc.hdr_bits = 1; bc.coded = false; bc.pad_to = 0;
+        h.hdr = 0; h.hdr_bits = 1; h.coded = false; h.pad_to = 0;
         return;
       }
-      bc.hdr = 1 | ((uint64_t)e << 2);
+      h.hdr = 1 | ((uint64_t)e << 2);
       outer = 2 + T::kEBits;
     } else {                                       // reinterpret sign-magnitude as two's complement
 #pragma unroll (N <= 64 ? N : 1)
       for (int i = 0; i < N; i++) v[i] = (I)raw[i] < 0 ? (I)(raw[i] ^ kTc) : (I)raw[i];
-      bc.hdr = 3;
+      h.hdr = 3;
       outer = 2;
     }
     xform<kRevFwd, D>(v);
     reorder<D>(v, u);
     const unsigned prec = rev_precision<U, N>(u, p.maxprec);
-    bc.hdr |= (uint64_t)(prec - 1) << outer;
-    bc.hdr_bits = outer + T::kPBits;
-    bc.budget = p.maxbits - outer - T::kPBits;
-    bc.maxprec = prec;
-    set_coeffs(bc, u);
+    h.hdr |= (uint64_t)(prec - 1) << outer;
+    h.hdr_bits = outer + T::kPBits;
+    h.budget = p.maxbits - outer - T::kPBits;
+    h.maxprec = prec;
   } else {
 #pragma unroll (N <= 64 ? N : 1)
     for (int i = 0; i < N; i++) v[i] = (I)raw[i];
     if (!rev) {
-      bc.hdr = 0; bc.hdr_bits = 0;
-      bc.budget = p.maxbits;
-      bc.maxprec = p.maxprec;
+      h.hdr = 0; h.hdr_bits = 0;
+      h.budget = p.maxbits;
+      h.maxprec = p.maxprec;
       xform<kFwd, D>(v);
       reorder<D>(v, u);
-      set_coeffs(bc, u);
     } else {
       xform<kRevFwd, D>(v);
       reorder<D>(v, u);
       const unsigned prec = rev_precision<U, N>(u, p.maxprec);
-      bc.hdr = prec - 1;
-      bc.hdr_bits = T::kPBits;
-      bc.budget = p.maxbits - T::kPBits;
-      bc.maxprec = prec;
-      set_coeffs(bc, u);
+      h.hdr = prec - 1;
+      h.hdr_bits = T::kPBits;
+      h.budget = p.maxbits - T::kPBits;
+      h.maxprec = prec;
     }
   }
 }
 
+// ---------------------------------------------------------------------------
+// plane-array coder (N <= 64): planes live in an array plane[k * stride]
+// (shared memory in the kernels, a local array on the host), the coder is a
+// rolled loop over planes.  Because the stream of a plane depends only on
+// the plane word and the count n of coefficients already significant, its
+// length is known in O(1) (popc/clz) and every plane that fits the budget is
+// written with no per-bit budget test; only the plane where the budget ends
+// takes the bit-exact truncating path.
+
+// bits of plane x given n significant coefficients; updates n
+template <int N>
+ZG_HD unsigned plane_bits(uint64_t x, unsigned& n) {
+  unsigned len = n;
+  if (n < (unsigned)N) {
+    const uint64_t r = x >> n;
+    if (!r) {
+      len += 1;
+    } else {
+      const unsigned hb = 63 - (unsigned)clz64(r);
+      const unsigned ones = (unsigned)popc64(r);
+      len += hb + 1 + ones;
+      if (n + hb + 1 < (unsigned)N) len += 1;   // closing negative group test
+      else len -= 1;                            // last coefficient's one is implied
+      n += hb + 1;
+    }
+  }
+  return len;
+}
+
+// write plane x completely (it fits the budget)
+template <int N, class Sink>
+ZG_HD void put_plane(Sink& out, uint64_t x, unsigned& n) {
+  out.put(n ? x & (~0ull >> (64 - n)) : 0ull, n);
+  if (n >= (unsigned)N) return;
+  uint64_t r = x >> n;
+  while (r) {
+    const unsigned z = ctz64(r);
+    if (n + z == (unsigned)N - 1) {   // positive test, z zeros, implied one
+      out.put(1, z + 1);
+      n = N;
+      return;
+    }
+    out.put(1 | (2ull << z), z + 2);  // positive test, z zeros, the one
+    n += z + 1;
+    r >>= z + 1;
+  }
+  out.put(0, 1);                      // negative test: rest of the plane is zero
+}
+
+// write the first `bits` bits of plane x's code (the budget ends inside it)
+template <int N, class Sink>
+ZG_HD void put_plane_cut(Sink& out, uint64_t x, unsigned n, unsigned bits) {
+  const unsigned m = n < bits ? n : bits;
+  out.put(m ? x & (~0ull >> (64 - m)) : 0ull, m);
+  bits -= m;
+  if (n >= (unsigned)N) return;
+  uint64_t r = x >> n;
+  while (bits) {
+    bits--;
+    if (!r) { out.put(0, 1); return; }
+    out.put(1, 1);
+    const unsigned z = ctz64(r);
+    if (n + z == (unsigned)N - 1) {
+      out.put(0, z < bits ? z : bits);
+      return;
+    }
+    const unsigned len = z + 1, e = len < bits ? len : bits;
+    out.put(e > z ? (1ull << z) : 0ull, e);
+    bits -= e;
+    if (e < len) return;
+    n += len;
+    r >>= len;
+  }
+}
+
+// total bits of a prepared block
+template <int P, int N>
+ZG_HD unsigned block_bits(const BlockHead& h, const uint64_t* plane, int stride) {
+  unsigned bits = h.hdr_bits;
+  if (h.coded) {
+    const int kmin = (unsigned)P > h.maxprec ? P - (int)h.maxprec : 0;
+    unsigned n = 0, code = 0;
+    for (int k = P - 1; k >= kmin && code < h.budget; k--) code += plane_bits<N>(plane[k * stride], n);
+    bits += code < h.budget ? code : h.budget;
+  }
+  return bits > h.pad_to ? bits : h.pad_to;
+}
+
+// write a prepared block; returns its bits
+template <int P, int N, class Sink>
+ZG_HD unsigned emit_block(Sink& out, const BlockHead& h, const uint64_t* plane, int stride) {
+  out.put(h.hdr, h.hdr_bits);
+  unsigned bits = h.hdr_bits;
+  if (h.coded) {
+    const int kmin = (unsigned)P > h.maxprec ? P - (int)h.maxprec : 0;
+    unsigned left = h.budget, n = 0;
+    for (int k = P - 1; k >= kmin && left; k--) {
+      const uint64_t x = plane[k * stride];
+      unsigned n2 = n;
+      const unsigned len = plane_bits<N>(x, n2);
+      if (len <= left) {
+        put_plane<N>(out, x, n);
+        left -= len;
+      } else {
+        put_plane_cut<N>(out, x, n, left);
+        left = 0;
+      }
+    }
+    bits += h.budget - left;
+  }
+  if (bits < h.pad_to) {
+    out.pad(h.pad_to - bits);
+    bits = h.pad_to;
+  }
+  return bits;
+}
+
+// coefficients -> planes stored at plane[k * stride]
+template <int N, typename U>
+ZG_HD void store_planes(const U (&u)[N], uint64_t* plane, int stride) {
+  constexpr int P = 8 * sizeof(U);
+  uint64_t pl[P];
+  make_planes<N>(u, pl);
+#pragma unroll
+  for (int k = 0; k < P; k++) plane[k * stride] = pl[k];
+}
+
+// 4D blocks keep the rolled wide coder over the coefficient array
+template <typename S>
+struct WideCode {
+  using U = typename Traits<S>::UInt;
+  BlockHead h;
+  U u[256];
+  template <class Sink>
+  ZG_HD unsigned emit(Sink& out) const {
+    out.put(h.hdr, h.hdr_bits);
+    unsigned bits = h.hdr_bits;
+    if (h.coded) bits += encode_planes_wide<U>(out, h.budget, h.maxprec, u);
+    if (bits < h.pad_to) { out.pad(h.pad_to - bits); bits = h.pad_to; }
+    return bits;
+  }
+  ZG_HD unsigned length() const {
+    CountSink c;
+    return emit(c);
+  }
+};
+
 template <typename S, int D, class Sink>
 ZG_HD unsigned encode_block(Sink& out, const BlockParams& p, const typename Traits<S>::Bits (&raw)[1 << (2 * D)]) {
-  BlockCode<S, D> bc;
-  prepare_block<S, D>(bc, p, raw);
-  return bc.emit(out);
+  using U = typename Traits<S>::UInt;
+  constexpr int N = 1 << (2 * D);
+  if constexpr (N <= 64) {
+    BlockHead h;
+    U u[N];
+    uint64_t plane[8 * sizeof(U)];
+    prepare_coeffs<S, D>(h, p, raw, u);
+    if (h.coded) store_planes<N>(u, plane, 1);
+    return emit_block<8 * sizeof(U), N>(out, h, plane, 1);
+  } else {
+    WideCode<S> wc;
+    prepare_coeffs<S, D>(wc.h, p, raw, wc.u);
+    return wc.emit(out);
+  }
 }
 
 template <typename S, int D, class Source>

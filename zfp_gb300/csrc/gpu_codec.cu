@@ -267,14 +267,14 @@ int persistent_grid() {
 }
 
 // decide shared- or global-memory staging and the grid
-static cudaError_t plan_launch(LaunchArgs& a, uint64_t bound_bits, uint32_t total_tiles, DevBuf& gimg,
-                               cudaStream_t st) {
+static cudaError_t plan_launch(LaunchArgs& a, uint64_t bound_bits, uint32_t total_tiles, size_t extra_smem,
+                               DevBuf& gimg, cudaStream_t st) {
   const uint64_t words = (uint64_t)kTile * bound_bits / 64 + 4;
   a.total_tiles = total_tiles;
   a.img_words = (uint32_t)words;
   a.gimg = nullptr;
   a.grid = (int)total_tiles;
-  if (words * 8 > kMaxTileSmem) {
+  if (words * 8 + extra_smem > kMaxTileSmem) {
     a.grid = (int)std::min<uint64_t>(total_tiles, (uint64_t)persistent_grid());
     cudaError_t e = gimg.alloc((size_t)a.grid * words * 8, st);
     if (e != cudaSuccess) return e;
@@ -413,7 +413,8 @@ size_t gpu_compress(zfp_stream* z, const zfp_field* f) {
   a.sc = lm.sc;
   a.use_ticket = fixed ? 0 : 1;
   DevBuf gimg;
-  if ((e = plan_launch(a, fixed ? z->maxbits : bound, job.ntiles, gimg, st)) != cudaSuccess ||
+  if ((e = plan_launch(a, fixed ? z->maxbits : bound, job.ntiles, plane_bytes(fi.esize, fi.dims), gimg, st)) !=
+          cudaSuccess ||
       (e = launch_encode_any(fi.type, fi.dims, a, st)) != cudaSuccess) {
     if (offsets) cudaFreeAsync(offsets, st);
     return fail_cuda("zfp_compress: launch", e);
@@ -576,7 +577,7 @@ size_t gpu_decompress(zfp_stream* z, zfp_field* f) {
   a.njobs = 1;
   a.sc = lm.sc;
   DevBuf gimg;
-  if ((e = plan_launch(a, fixed ? z->maxbits : bound, job.ntiles, gimg, st)) != cudaSuccess) {
+  if ((e = plan_launch(a, fixed ? z->maxbits : bound, job.ntiles, 0, gimg, st)) != cudaSuccess) {
     if (parsed) cudaFreeAsync(parsed, st);
     return fail_cuda("zfp_decompress: plan", e);
   }

@@ -185,9 +185,8 @@ struct SmemSink {
     }
     word++;
   }
+  // v must have no bits at or above n
   __device__ __forceinline__ void put(uint64_t v, unsigned n) {
-    if (!n) return;
-    v = low_bits(v, n);
     acc |= v << fill;
     const unsigned t = fill + n;
     if (t >= 64) {
@@ -341,9 +340,11 @@ __device__ __forceinline__ void write_tile(const Job& job, const LaunchScratch& 
 
 template <typename S, int D>
 __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch& sc, uint32_t gt, uint64_t* img,
-                                            uint32_t img_words) {
+                                            uint32_t img_words, uint64_t* planes) {
   using B = typename Traits<S>::Bits;
+  using U = typename Traits<S>::UInt;
   constexpr int N = 1 << (2 * D);
+  constexpr int P = 8 * sizeof(U);
   __shared__ uint32_t s_warp[kTile / 32];
   __shared__ unsigned long long s_base;
   const uint32_t lt = gt - job.tile0;
@@ -351,14 +352,24 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
   const bool active = b < job.nblocks;
   const bool fixed = job.flags & kFixedRate;
   const BlockParams p{job.minbits, job.maxbits, job.maxprec, job.minexp};
+  uint64_t* my_planes = planes + threadIdx.x;   // plane k of this block at my_planes[k * kTile]
 
-  BlockCode<S, D> bc;
+  uint32_t len = 0;
+  BlockHead h;
+  [[maybe_unused]] WideCode<S> wc;  // 4D only (local memory)
   if (active) {
     B raw[N];
     gather<B, D>(job, b, raw);
-    prepare_block<S, D>(bc, p, raw);
+    if constexpr (N <= 64) {
+      U u[N];
+      prepare_coeffs<S, D>(h, p, raw, u);
+      if (h.coded) store_planes<N>(u, my_planes, kTile);
+      len = fixed ? job.maxbits : block_bits<P, N>(h, my_planes, kTile);
+    } else {
+      prepare_coeffs<S, D>(wc.h, p, raw, wc.u);
+      len = fixed ? job.maxbits : wc.length();
+    }
   }
-  const uint32_t len = active ? (fixed ? job.maxbits : bc.length()) : 0u;
   uint32_t total;
   const uint32_t excl = cta_exclusive_scan(len, total, s_warp);
 
@@ -373,7 +384,8 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
   }
   if (active) {
     SmemSink out{img, excl >> 6, excl & 63u, 0ull, true, nw, &job.result->status};
-    bc.emit(out);
+    if constexpr (N <= 64) emit_block<P, N>(out, h, my_planes, kTile);
+    else wc.emit(out);
     out.finish();
   }
   __syncthreads();
@@ -382,6 +394,12 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
   write_tile(job, sc, lt, gt, img, nw, G, total);
   if (active && (job.flags & kWriteIndex)) job.offsets[b] = G + excl;
   if (threadIdx.x == 0 && lt + 1 == job.ntiles) job.result->end_bit = G + total;
+}
+
+// dynamic shared memory for the bit planes of one tile (1-3D blocks)
+template <typename S, int D>
+constexpr size_t plane_smem_bytes() {
+  return (1 << (2 * D)) <= 64 ? (size_t)8 * sizeof(typename Traits<S>::UInt) * kTile * 8 : 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -470,6 +488,7 @@ __global__ void __launch_bounds__(kTile) encode_kernel(const __grid_constant__ J
                                                        uint64_t* gimg, uint32_t img_words) {
   extern __shared__ uint64_t smem_img[];
   uint64_t* img = gimg ? gimg + (size_t)blockIdx.x * img_words : smem_img;
+  uint64_t* planes = smem_img + (gimg ? 0 : img_words);
   __shared__ uint32_t s_tile;
   __shared__ Job s_job;
   for (uint32_t iter = blockIdx.x;; iter += gridDim.x) {
@@ -478,7 +497,7 @@ __global__ void __launch_bounds__(kTile) encode_kernel(const __grid_constant__ J
     const uint32_t gt = s_tile;
     if (gt >= total_tiles) break;
     const Job* job = resolve_job<kMulti>(one, jobs, njobs, gt, &s_job);
-    encode_tile<S, D>(*job, sc, gt, img, img_words);
+    encode_tile<S, D>(*job, sc, gt, img, img_words, planes);
     __syncthreads();
   }
 }

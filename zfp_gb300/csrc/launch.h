@@ -26,7 +26,12 @@ template <typename S, int D> cudaError_t run_encode(const LaunchArgs& a, cudaStr
 template <typename S, int D> cudaError_t run_decode(const LaunchArgs& a, cudaStream_t st);
 template <typename S, int D> cudaError_t run_parse(const Job& job, cudaStream_t st);
 
-// largest dynamic shared memory a tile may use before staging moves to global memory
-constexpr size_t kMaxTileSmem = 160 * 1024;
+// dynamic shared memory a kernel may request (GB300: 227 KB per CTA)
+constexpr size_t kSmemLimit = 227 * 1024;
+// a tile image plus bit planes larger than this is staged in global memory instead
+constexpr size_t kMaxTileSmem = 216 * 1024;
+
+// shared memory the encoder keeps for bit planes: 1-3D blocks only
+inline size_t plane_bytes(size_t esize, int dims) { return dims <= 3 ? esize * 8 * kTile * 8 : 0; }
 
 }  // namespace zg

@@ -9,13 +9,13 @@ namespace zg {
 
 template <class K>
 static void allow_smem(K kernel) {
-  // once per kernel: let it use up to kMaxTileSmem of dynamic shared memory
-  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxTileSmem);
+  // once per kernel: let it use the whole shared memory of an SM
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit);
 }
 
 template <typename S, int D>
 cudaError_t run_encode(const LaunchArgs& a, cudaStream_t st) {
-  const size_t smem = a.gimg ? 0 : (size_t)a.img_words * 8;
+  const size_t smem = (a.gimg ? 0 : (size_t)a.img_words * 8) + plane_smem_bytes<S, D>();
   if (a.jobs) {  // device job array: the multi-job kernel
     static const bool once = (allow_smem(encode_kernel<S, D, true>), true);
     (void)once;
