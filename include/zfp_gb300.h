@@ -64,6 +64,24 @@ void zfp_gb300_batch_free(zfp_gb300_batch* batch);
  * the built-in autotuner measured fastest for this batch on its first run. */
 zfp_bool zfp_gb300_batch_set_ctas_per_sm(zfp_gb300_batch* batch, int ctas_per_sm);
 
+/* ---- compression without device allocation -----------------------------
+ * No counterpart in the reference: zfp_compress there has no GPU scratch.
+ * Same stream as zfp_compress (zfp_exec_cuda), for callers that cannot let
+ * the library allocate device memory -- for example a program whose device
+ * memory belongs to another allocator, or a latency-critical loop that must
+ * not trigger an allocation.  Field and stream buffers must be in device
+ * memory; nothing is staged, and the encoder's scratch is a fixed 1 MiB
+ * device array inside the library (held by every GPU that loads it), which
+ * limits a call to 4,194,304 zfp blocks (e.g. 512^3 float) and to blocks
+ * whose tile fits shared memory.  Larger or host-resident inputs return 0
+ * with a reason in zfp_gb300_last_error().  The first call on a device
+ * looks up that array's device address; make that first call before any
+ * CUDA stream capture.  All calls share the array: calls whose GPU work
+ * overlaps (other CUDA streams or host threads) race and must be ordered by
+ * the caller.  No block index is kept, so zfp_decompress of a variable-rate
+ * stream written here recovers block offsets by parsing the stream. */
+size_t zfp_gb300_compress_noalloc(zfp_stream* zfp, const zfp_field* field);
+
 #ifdef __cplusplus
 }
 #endif

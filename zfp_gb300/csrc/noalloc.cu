@@ -1,0 +1,127 @@
+// noalloc.cu -- zfp_compress for callers that cannot allocate device memory.
+//
+// zfp_compress allocates: staging buffers for host data, the per-launch
+// scratch of the encoder (tile states for the variable-rate look-back,
+// boundary words shared by neighbouring tiles, the tile counter) and the
+// block index it keeps for later decompression.  Some callers cannot let a
+// library call cudaMalloc or cudaMallocAsync: programs whose device memory
+// is entirely owned by another allocator (a framework's caching allocator
+// that has reserved the pool), and latency-critical loops that must not
+// trigger the implicit synchronisation or pool growth an allocation can
+// cause.  zfp_gb300_compress_noalloc serves them: the caller passes device
+// field and stream buffers, and the encoder's scratch lives in one
+// file-scope device array of fixed size instead of being allocated.
+//
+// The array is shared by every call in the process on a given device and
+// keeps what the last call left in it; each call clears the part it uses
+// before launching.  Two calls whose GPU work overlaps in time (different
+// CUDA streams, or different host threads) race on it and must be ordered
+// by the caller.  Every GPU that loads the library holds the array until
+// the process exits.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <mutex>
+
+#include "../../include/zfp_gb300.h"
+#include "gpu_internal.h"
+#include "runtime.h"
+
+namespace zg {
+
+// up to this many tiles of kTile blocks per call (4,194,304 blocks)
+constexpr uint32_t kNoAllocMaxTiles = 32768;
+constexpr size_t kNoAllocBytes = 1u << 20;  // 1 MiB per device
+static_assert(64 + ((size_t)kNoAllocMaxTiles + 1) * 28 <= kNoAllocBytes, "scratch layout does not fit");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_addr[256];  // per device ordinal, resolved on the first call on that device
+
+// Device address of g_noalloc_scratch on the current device.  In host code
+// the array's name is only a host-side handle, so the address is looked up
+// once per device with cudaGetSymbolAddress while that device is current.
+static void* noalloc_scratch(cudaError_t& err) {
+  int dev = 0;
+  err = cudaGetDevice(&dev);
+  if (err != cudaSuccess || dev < 0 || dev >= 256) return nullptr;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (err != cudaSuccess) return nullptr;
+    g_noalloc_addr[dev] = p;
+  }
+  return g_noalloc_addr[dev];
+}
+
+}  // namespace zg
+
+extern "C" size_t zfp_gb300_compress_noalloc(zfp_stream* z, const zfp_field* f) {
+  using namespace zg;
+  ExecParams* ep = exec_params(z);
+  if (!ep) return fail("zfp_gb300_compress_noalloc: the stream's execution policy is not zfp_exec_cuda");
+  if (!z->stream) return fail("zfp_gb300_compress_noalloc: no bit stream");
+  FieldInfo fi;
+  if (const char* why = field_info(f, fi)) return fail(why);
+  const StreamState ss = get_stream_state(z->stream);
+  if (!ss.begin || !is_device_ptr(ss.begin) || !is_device_ptr(f->data))
+    return fail("zfp_gb300_compress_noalloc: field and stream must be in device memory");
+  const uint64_t ntiles = (fi.nblocks + kTile - 1) / kTile;
+  if (ntiles > kNoAllocMaxTiles)
+    return fail("zfp_gb300_compress_noalloc: field has more than 4194304 blocks (the scratch limit)");
+  const bool fixed = is_fixed_rate(fi, z);
+  const uint64_t bound = fixed ? (uint64_t)z->maxbits : block_bound(fi, z);
+  const uint64_t img_words = (uint64_t)kTile * bound / 64 + 4;
+  if (img_words * 8 + plane_bytes(fi.esize, fi.dims) > kMaxTileSmem)
+    return fail("zfp_gb300_compress_noalloc: blocks too large for shared-memory staging");
+  const uint64_t bit0 = (uint64_t)(ss.ptr - ss.begin) * 64 + ss.bits;
+  const uint64_t cap_words = (uint64_t)(ss.end - ss.begin);
+  if (fixed && (bit0 + fi.nblocks * (uint64_t)z->maxbits + 63) / 64 > cap_words)
+    return fail("zfp_gb300_compress_noalloc: stream buffer too small");
+
+  cudaError_t e;
+  char* scratch = (char*)noalloc_scratch(e);
+  if (!scratch) return fail_cuda("zfp_gb300_compress_noalloc: cudaGetSymbolAddress", e);
+  const cudaStream_t st = ep->stream;
+  const size_t t = (size_t)ntiles + 1;
+  const size_t used = 64 + t * 28;
+  // the previous call's state must not leak into this one
+  if ((e = cudaMemsetAsync(scratch, 0, used, st)) != cudaSuccess)
+    return fail_cuda("zfp_gb300_compress_noalloc: clear scratch", e);
+
+  Job job = base_job(fi, z, f->data);
+  job.flags = (fixed ? kFixedRate : 0u) | (vector_ok(fi, f->data) ? kVecOk : 0u);
+  job.words = ss.begin;
+  job.cap_words = cap_words;
+  job.bit0 = bit0;
+  job.head_word = ss.bits ? (ss.buffer & ((1ull << ss.bits) - 1)) : 0;
+  job.result = (JobResult*)scratch;
+
+  LaunchArgs a;
+  std::memset(&a, 0, sizeof a);
+  a.one = job;
+  a.njobs = 1;
+  a.sc.ticket = (unsigned int*)(scratch + 32);
+  a.sc.tile_state = (unsigned long long*)(scratch + 64);
+  a.sc.side = (unsigned long long*)(scratch + 64 + t * 8);
+  a.sc.side_cnt = (unsigned int*)(scratch + 64 + t * 24);
+  a.total_tiles = (uint32_t)ntiles;
+  a.use_ticket = fixed ? 0 : 1;
+  a.img_words = (uint32_t)img_words;
+  a.grid = (int)ntiles;
+  if ((e = launch_encode_any(fi.type, fi.dims, a, st)) != cudaSuccess)
+    return fail_cuda("zfp_gb300_compress_noalloc: launch", e);
+
+  JobResult res;
+  if ((e = cudaMemcpyAsync(&res, scratch, sizeof res, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(st)) != cudaSuccess)
+    return fail_cuda("zfp_gb300_compress_noalloc: kernel", e);
+  if (res.status)
+    return fail(res.status & kStatusOverflow ? "zfp_gb300_compress_noalloc: stream buffer too small"
+                                             : "zfp_gb300_compress_noalloc: GPU wait timed out");
+  set_stream_flushed(z->stream, res.end_bit);
+  set_error("");
+  return (size_t)((res.end_bit + 63) / 64) * 8;
+}
