@@ -17,6 +17,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes as C
+import faulthandler
 import json
 import os
 import statistics
@@ -48,6 +49,7 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-batch", action="store_true")
+    p.add_argument("--no-serve", action="store_true")
     p.add_argument("--only", default=None,
                    help="profiling: run one kernel, FIELD:MODE:DIR (e.g. f32:rate:c), --steps times")
     p.add_argument("--shape", default=None, help="profiling: field shape Z,Y,X for --only")
@@ -59,6 +61,25 @@ def dist_info():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def job_ms(ms_local: float, world: int, device: str) -> float:
+    """Length of the timed region of the whole job: the slowest rank's
+    milliseconds (all-reduce MAX, then a barrier so no rank leaves early)."""
+    if world <= 1:
+        return ms_local
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms_local], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def job_gbs(raw_bytes_per_step: int, steps: int, world: int, ms: float) -> float:
+    """Whole-job throughput: every rank codes the same bytes per step (weak
+    scaling), so the job moved world x steps x bytes in the slowest rank's time."""
+    return world * raw_bytes_per_step * steps / (ms / 1e3) / 1e9
 
 
 def field_shapes(small: bool):
@@ -272,14 +293,9 @@ def gpu_arm(args):
             step()
         e1.record(stream)
         torch.cuda.synchronize()
-    ms_total = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms_total], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = t.item()
-        dist.barrier()
+    ms_total = job_ms(e0.elapsed_time(e1), world, "cuda")
     raw_step = sum(2 * fd["raw"] * len(MODES) for fd in fields)
-    value = world * raw_step * args.steps / (ms_total / 1e3) / 1e9
+    value = job_gbs(raw_step, args.steps, world, ms_total)
     launches = 2 * len(MODES) * len(fields) * args.steps
 
     # roofline of the dominant kernel
@@ -309,6 +325,11 @@ def gpu_arm(args):
         torch.cuda.empty_cache()
         batch = batch_compare(lib, torch, stream, args)
 
+    serving = None
+    if not args.no_serve:
+        torch.cuda.empty_cache()
+        serving = serve_compare(lib, torch, args)
+
     if rank == 0:
         clocks = clk.summary()
         line = {
@@ -327,6 +348,7 @@ def gpu_arm(args):
             "checks": checks,
             "compression_ratio": ratios,
             "batch": batch,
+            "serving": serving,
         }
         print(json.dumps(line))
     if world > 1:
@@ -443,6 +465,198 @@ def batch_compare(lib, torch, stream, args):
                         "speedup": round(per_s / bat_s, 2), "bit_identical": bool(same),
                         "per_array_ms": round(per_s * 1e3, 3), "batched_ms": round(bat_s * 1e3, 3)}
     return result
+
+
+def serve_compare(lib, torch, args):
+    """Configuration 5: a Poisson stream of requests (70% compress, 30%
+    decompress), each a 2D or 3D float32/float64 field whose raw size is
+    log-uniform in [16 KiB, 256 MiB] (smooth-field generator, seed 3),
+    fixed-accuracy tolerance 1e-4 x the field's range.  Served by the
+    continuous-batching server under a 64 GiB HBM budget, and by one worker
+    calling zfp_compress / zfp_decompress per request on the same arrival
+    schedule.  Fields are views of resident generated fields; decompress
+    requests read streams compressed before the timed run."""
+    import queue
+
+    from zfp_gb300 import capi, synth
+    L = lib.lib
+    L.zfp_gb300_server_create.restype = C.c_void_p
+    L.zfp_gb300_server_create.argtypes = [C.c_size_t, C.c_int]
+    L.zfp_gb300_server_submit.restype = C.c_uint64
+    L.zfp_gb300_server_submit.argtypes = [C.c_void_p, capi.PZ, capi.PF, C.c_int]
+    L.zfp_gb300_server_wait.restype = C.c_size_t
+    L.zfp_gb300_server_wait.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(C.c_double)]
+    L.zfp_gb300_server_free.argtypes = [C.c_void_p]
+    rng = np.random.default_rng(3)
+    count = 20000 if not args.small else 600
+    smax = (256 << 20) if not args.small else (8 << 20)
+    rate = 6000.0 if not args.small else 2000.0
+    bases = {}
+    for dt, esz in ((torch.float32, 4), (torch.float64, 8)):
+        for dims in (2, 3):
+            side = int((smax / esz) ** (1.0 / dims)) + 1
+            bases[(esz, dims)] = synth.smooth_field_torch((side,) * dims, dt, seed=3 + esz + dims, noise=1e-2)
+    def random_field():
+        esz = 4 if rng.random() < 0.5 else 8
+        dims = 2 if rng.random() < 0.5 else 3
+        size = float(np.exp(rng.uniform(np.log(16 << 10), np.log(smax))))
+        base = bases[(esz, dims)]
+        n = max(4, min(base.shape[0], int(round((size / esz) ** (1.0 / dims)))))
+        view = base[(slice(0, n),) * dims]
+        lo, hi = torch.aminmax(view)
+        return dict(view=view, esz=esz, dims=dims, tol=1e-4 * float(hi - lo), raw=view.numel() * esz)
+
+    # decompress requests draw from 64 templates (same size distribution), each compressed once
+    templates = [random_field() for _ in range(64)]
+    reqs = []
+    for i in range(count):
+        if rng.random() < 0.7:
+            reqs.append(dict(random_field(), direction=0))
+        else:
+            t = int(rng.integers(len(templates)))
+            reqs.append(dict(templates[t], direction=1, template=t))
+    total_raw = sum(r["raw"] for r in reqs)
+    gaps = rng.exponential(1.0 / rate, size=count)
+    arrivals = np.cumsum(gaps) - gaps[0]
+
+    def make_objects(r, buf_ptr, nbytes, out_ptr=None):
+        bs = lib.stream_open(buf_ptr, nbytes)
+        z = lib.zfp_stream_open(bs)
+        zt = capi.TYPE_FLOAT if r["esz"] == 4 else capi.TYPE_DOUBLE
+        lib.zfp_stream_set_accuracy(z, r["tol"])
+        lib.zfp_stream_set_execution(z, capi.EXEC_CUDA)
+        v = r["view"]
+        n = tuple(reversed(v.shape))
+        st = tuple(reversed(v.stride()))
+        f = capi.make_field(lib, out_ptr if out_ptr is not None else v.data_ptr(), zt, n,
+                            st if out_ptr is None else ())
+        return bs, z, f
+
+    def max_bytes(r):
+        bs, z, f = make_objects(r, 0, 0)
+        m = lib.zfp_stream_maximum_size(z, f)
+        lib.zfp_field_free(f)
+        lib.zfp_stream_close(z)
+        lib.stream_close(bs)
+        return m
+
+    # output buffers: a ring per direction (requests that share a slot overwrite each other's
+    # output; only the timing of this experiment is measured, the parity test is separate)
+    ring = 48 if not args.small else 16
+    worst = max_bytes(max(reqs, key=lambda r: r["raw"])) + 4096
+    cbufs = [torch.empty(worst // 8 + 8, dtype=torch.int64, device="cuda") for _ in range(ring)]
+    outs = {k: [torch.empty_like(v) for _ in range(4)] for k, v in bases.items()}
+    dstreams = []
+    for r in templates:
+        m = max_bytes(r)
+        buf = torch.empty(m // 8 + 8, dtype=torch.int64, device="cuda")
+        bs, z, f = make_objects(r, buf.data_ptr(), m)
+        assert lib.zfp_compress(z, f)
+        lib.zfp_field_free(f)
+        lib.zfp_stream_close(z)
+        lib.stream_close(bs)
+        dstreams.append((buf, m))
+    objs = []
+    for i, r in enumerate(reqs):
+        if r["direction"] == 0:
+            buf = cbufs[i % ring]
+            objs.append(make_objects(r, buf.data_ptr(), max_bytes(r)))
+        else:
+            buf, m = dstreams[r["template"]]
+            out = outs[(r["esz"], r["dims"])][i % 4]
+            objs.append(make_objects(r, buf.data_ptr(), m, out_ptr=out.data_ptr()))
+    torch.cuda.synchronize()
+
+    def run(submit_fn, wait_fn):
+        lat = [0.0] * count
+        q = queue.Queue()
+        t0 = time.perf_counter() + 0.05
+
+        def waiter():
+            for _ in range(count):
+                i, tk = q.get()
+                lat[i] = wait_fn(i, tk)
+        th = threading.Thread(target=waiter)
+        th.start()
+        for i in range(count):
+            delay = t0 + arrivals[i] - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            q.put((i, submit_fn(i)))
+        th.join()
+        return lat, time.perf_counter() - t0
+
+    # continuous batching server
+    server = L.zfp_gb300_server_create(64 << 30, 4)
+    secs = C.c_double()
+
+    def s_submit(i):
+        bs, z, f = objs[i]
+        lib.zfp_stream_rewind(z)
+        return L.zfp_gb300_server_submit(server, z, f, reqs[i]["direction"])
+
+    failed = []
+
+    def s_wait(i, tk):
+        if not tk or not L.zfp_gb300_server_wait(server, tk, C.byref(secs)):
+            failed.append((i, zfp_gb300_last()))
+            return float("nan")
+        return secs.value
+
+    lat_s, wall_s = run(s_submit, s_wait)
+    L.zfp_gb300_server_free(server)
+
+    # per-request GPU path on the same schedule: one worker, one call per request
+    work = queue.Queue()
+    done_at = [0.0] * count
+
+    def worker():
+        while True:
+            item = work.get()
+            if item is None:
+                return
+            i = item
+            bs, z, f = objs[i]
+            lib.zfp_stream_rewind(z)
+            fn = lib.zfp_compress if reqs[i]["direction"] == 0 else lib.zfp_decompress
+            assert fn(z, f)
+            done_at[i] = time.perf_counter()
+
+    wth = threading.Thread(target=worker)
+    wth.start()
+    sub_at = [0.0] * count
+
+    def p_submit(i):
+        sub_at[i] = time.perf_counter()
+        work.put(i)
+        return i
+
+    def p_wait(i, tk):
+        while not done_at[i]:
+            time.sleep(5e-5)
+        return done_at[i] - sub_at[i]
+
+    lat_p, wall_p = run(p_submit, p_wait)
+    work.put(None)
+    wth.join()
+    for bs, z, f in objs:
+        lib.zfp_field_free(f)
+        lib.zfp_stream_close(z)
+        lib.stream_close(bs)
+
+    def pct(a, q):
+        return round(float(np.nanpercentile(np.array(a) * 1e3, q)), 3)
+    return {"requests": count, "mean_rate_per_s": rate, "hbm_budget_gib": 64, "lanes": 4, "raw_bytes": total_raw,
+            "server": {"p50_ms": pct(lat_s, 50), "p99_ms": pct(lat_s, 99), "sustained_gbs": round(total_raw / wall_s / 1e9, 2),
+                       "wall_s": round(wall_s, 3), "failed": len(failed),
+                       "first_failure": failed[0][1] if failed else None},
+            "per_request": {"p50_ms": pct(lat_p, 50), "p99_ms": pct(lat_p, 99),
+                            "sustained_gbs": round(total_raw / wall_p / 1e9, 2), "wall_s": round(wall_p, 3)}}
+
+
+def zfp_gb300_last():
+    import zfp_gb300
+    return zfp_gb300.last_error()
 
 
 def e2e_run(lib, torch, codec, fields, args):
@@ -592,6 +806,7 @@ def profile_one(args):
 
 
 def main():
+    faulthandler.enable()
     args = parse_args()
     if args.only:
         profile_one(args)

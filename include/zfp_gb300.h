@@ -64,6 +64,36 @@ void zfp_gb300_batch_free(zfp_gb300_batch* batch);
  * the built-in autotuner measured fastest for this batch on its first run. */
 zfp_bool zfp_gb300_batch_set_ctas_per_sm(zfp_gb300_batch* batch, int ctas_per_sm);
 
+/* ---- serving: continuous batching of independent requests --------------
+ * A server runs compress / decompress requests on device-resident fields
+ * and streams as they arrive.  A dispatcher thread keeps `lanes` CUDA
+ * streams busy: whenever a lane is free it admits waiting requests in
+ * arrival order while the bytes of all admitted, unfinished requests (field
+ * span plus stream capacity) stay within `hbm_budget`, and launches them as
+ * one batch (one persistent launch per scalar type and dimensionality).
+ * Requests that arrive while batches run join the next batch on the next
+ * free lane, so work from different batches overlaps on the GPU.  Results
+ * are the same streams/arrays zfp_compress / zfp_decompress produce. */
+typedef struct zfp_gb300_server zfp_gb300_server;
+
+zfp_gb300_server* zfp_gb300_server_create(size_t hbm_budget, int lanes);
+
+/* direction 0 = compress, 1 = decompress.  Returns a ticket (> 0), or 0 if
+ * the request cannot be served (host memory, larger than the budget, ...).
+ * The zfp_stream, its bit stream and the field must stay valid until the
+ * request has been waited for. */
+uint64_t zfp_gb300_server_submit(zfp_gb300_server* server, zfp_stream* zfp, const zfp_field* field,
+                                 int direction);
+
+/* Block until the request is done; leaves its bit stream as zfp_compress /
+ * zfp_decompress would and returns the stream size in bytes (0 on failure).
+ * If seconds is not NULL it receives the time from submission to the end of
+ * the request's GPU work. */
+size_t zfp_gb300_server_wait(zfp_gb300_server* server, uint64_t ticket, double* seconds);
+
+/* Finish everything submitted, stop the dispatcher and release the server. */
+void zfp_gb300_server_free(zfp_gb300_server* server);
+
 /* ---- compression without device allocation -----------------------------
  * No counterpart in the reference: zfp_compress there has no GPU scratch.
  * Same stream as zfp_compress (zfp_exec_cuda), for callers that cannot let

@@ -10,12 +10,19 @@
 
 namespace {
 
+// Like the kernels' sinks, put() requires v to have no bits at or above n;
+// a violation is recorded (and makes the field compare fail) instead of
+// being masked away.
+static bool g_unclean_put = false;
+
 struct VecSink {
   uint64_t* words;
   uint64_t pos;
   ZG_HD void put(uint64_t v, unsigned n) {
+#if !defined(__CUDA_ARCH__)
+    if (n < 64 && (v >> n)) g_unclean_put = true;
+#endif
     if (!n) return;
-    v = zg::low_bits(v, n);
     const unsigned o = (unsigned)(pos & 63);
     words[pos >> 6] |= v << o;
     if (o && o + n > 64) words[(pos >> 6) + 1] |= v >> (64 - o);
@@ -136,6 +143,12 @@ uint64_t decompress_s(const Geom& g, const zg::BlockParams& p, void* d, const ui
 }
 
 }  // namespace
+
+extern "C" int zgh_unclean_put(void) {
+  const int r = g_unclean_put;
+  g_unclean_put = false;
+  return r;
+}
 
 extern "C" uint64_t zgh_compress(int type, int dims, const size_t* n, const ptrdiff_t* s,
                                  const void* data, const unsigned* prm, uint64_t* words, uint64_t bit0) {

@@ -89,6 +89,7 @@ def test_device_codec_on_host_matches_oracle(host, oracle, dims, dtype):
             w1, e1 = host_compress(host, oracle, view, prm, bit0)
             nw = (e0 + 63) // 64
             assert e0 == e1 and np.array_equal(w0[:nw], w1[:nw]), (mode, arg, shape, trial)
+            assert not host.zgh_unclean_put(), ("a sink received bits above its length", mode, arg, shape)
             d0 = np.zeros(view.shape, dtype=dtype)
             d1 = np.zeros(view.shape, dtype=dtype)
             x0 = oracle.decompress(w0[: nw + 2], d0, prm, bit0)

@@ -50,7 +50,7 @@ struct zfp_gb300_batch {
   zg::JobResult* d_results = nullptr;
   uint64_t* d_offsets = nullptr;       // compress: concatenated per-block indexes of variable-rate jobs
   std::vector<size_t> offset_base;     // per job: first entry in d_offsets (or SIZE_MAX)
-  std::vector<uint64_t*> parsed;       // decompress: indexes recovered by parsing (owned)
+  std::vector<zg::IndexRef> held;      // decompress: indexes this batch reads (kept until it is freed)
   cudaStream_t own_stream = nullptr;
   cudaStream_t last_stream = nullptr;
   cudaGraphExec_t graph = nullptr;
@@ -99,7 +99,7 @@ static void destroy(zfp_gb300_batch* b) {
   }
   cudaFree(b->d_results);
   cudaFree(b->d_offsets);
-  for (uint64_t* p : b->parsed) cudaFree(p);
+  b->held.clear();
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   delete b;
 }
@@ -176,22 +176,22 @@ zfp_gb300_batch* zfp_gb300_batch_create(zfp_stream* const* streams, const zfp_fi
         b->nominal_end[i] = j.bit0 + fi.nblocks * (uint64_t)z->maxbits;
       } else {
         IndexEntry ent;
-        if (registry_find(ss.begin, j.bit0, fi, z, nullptr, ent)) {
-          j.offsets = ent.offsets;
+        if (registry_find(ss.begin, j.bit0, fi, z, ent)) {
+          j.offsets = ent.index->ptr;
           j.end_bit = ent.end_bit;
           j.flags |= kVerify;
+          b->held.push_back(ent.index);
         } else {
           // stream written elsewhere: recover its block offsets now
-          uint64_t* offs = nullptr;
           JobResult r{};
-          if ((e = cudaMalloc((void**)&offs, fi.nblocks * 8)) != cudaSuccess) {
+          IndexRef idx = make_index(fi.nblocks, nullptr, e);
+          if (!idx) {
             fail_cuda("zfp_gb300_batch_create: index", e);
             destroy(b);
             return nullptr;
           }
-          b->parsed.push_back(offs);
           Job pj = j;
-          pj.offsets = offs;
+          pj.offsets = idx->ptr;
           if ((e = cudaMemset(j.result, 0, sizeof(JobResult))) != cudaSuccess ||
               (e = launch_parse_any(fi.type, fi.dims, pj, nullptr)) != cudaSuccess ||
               (e = cudaMemcpy(&r, j.result, sizeof r, cudaMemcpyDeviceToHost)) != cudaSuccess) {
@@ -199,8 +199,10 @@ zfp_gb300_batch* zfp_gb300_batch_create(zfp_stream* const* streams, const zfp_fi
             destroy(b);
             return nullptr;
           }
-          j.offsets = offs;
+          j.offsets = idx->ptr;
           j.end_bit = r.end_bit;
+          b->held.push_back(idx);
+          registry_insert(make_entry(ss.begin, j.bit0, r.end_bit, fi, j, idx));
         }
       }
     }
@@ -246,7 +248,7 @@ zfp_gb300_batch* zfp_gb300_batch_create(zfp_stream* const* streams, const zfp_fi
     g.sc.tile_state = (unsigned long long*)(p + 64);
     g.sc.side = (unsigned long long*)(p + 64 + t * 8);
     g.sc.side_cnt = (unsigned int*)(p + 64 + t * 24);
-    const size_t extra = b->direction == 0 ? plane_bytes(b->info[g.members[0]].esize, g.dims) : 0;
+    const size_t extra = plane_bytes(b->info[g.members[0]].esize, g.dims);
     if ((size_t)g.img_words * 8 + extra > kMaxTileSmem) {
       g.gimg_words = (size_t)persistent_grid() * 2 * g.img_words;
       if ((e = cudaMalloc((void**)&g.gimg, g.gimg_words * 8)) != cudaSuccess) {
@@ -376,24 +378,15 @@ zfp_bool zfp_gb300_batch_finish(zfp_gb300_batch* b, size_t* sizes) {
       end = fixed ? b->nominal_end[i] : res[i].end_bit;
       const StreamState ss = get_stream_state(b->streams[i]->stream);
       if (!fixed) {  // keep the block index for later decompression of this stream
-        IndexEntry ne;
-        ne.begin = ss.begin;
-        ne.bit0 = j.bit0;
-        ne.end_bit = end;
-        ne.nblocks = j.nblocks;
-        ne.type = b->info[i].type;
-        ne.dims = b->info[i].dims;
-        ne.minbits = j.minbits;
-        ne.maxbits = j.maxbits;
-        ne.maxprec = j.maxprec;
-        ne.minexp = j.minexp;
-        ne.stream = b->last_stream;
-        ne.tick = 0;
-        ne.offsets = nullptr;
-        if (cudaMallocAsync((void**)&ne.offsets, j.nblocks * 8, b->last_stream) == cudaSuccess &&
-            cudaMemcpyAsync(ne.offsets, j.offsets, j.nblocks * 8, cudaMemcpyDeviceToDevice, b->last_stream) ==
-                cudaSuccess)
-          registry_insert(ne);
+        cudaError_t ie;
+        IndexRef idx = make_index(j.nblocks, b->last_stream, ie);
+        if (idx && cudaMemcpyAsync(idx->ptr, j.offsets, j.nblocks * 8, cudaMemcpyDeviceToDevice, b->last_stream) ==
+                       cudaSuccess &&
+            cudaEventCreateWithFlags(&idx->written, cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventRecord(idx->written, b->last_stream) == cudaSuccess)
+          registry_insert(make_entry(ss.begin, j.bit0, end, b->info[i], j, idx));
+        else
+          cudaGetLastError();
       } else {
         registry_invalidate(ss.begin, j.bit0, end);
       }

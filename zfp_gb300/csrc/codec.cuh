@@ -65,6 +65,16 @@ struct BlockParams {
   int32_t minexp;
 };
 
+// Which code paths a kernel carries: both (jobs of mixed modes), or only
+// the lossy / only the reversible one -- each specialisation keeps the
+// other path's registers out of the kernel.
+enum ModeSel { kAnyMode = 0, kLossyOnly = 1, kRevOnly = 2 };
+
+template <int kSel>
+ZG_HD bool is_rev(const BlockParams& p) {
+  return kSel == kRevOnly || (kSel == kAnyMode && p.minexp < kMinExp);
+}
+
 // ---------------------------------------------------------------------------
 // bit helpers with host equivalents
 
@@ -539,36 +549,53 @@ ZG_HD unsigned encode_planes(Sink& out, unsigned budget, unsigned maxprec, const
   return budget - bits;
 }
 
-// Decoder twin (src/template/decode.c:80-278).  When the budget ends inside
-// a positive group test the reference still deposits a one at the scan
-// position; so does this.
+// Decoder twin (src/template/decode.c:80-278), rolled over planes; plane k
+// is stored to pb.p[k * pb.stride] (planes not reached are zeroed).  A
+// positive group test and the scan that follows it are read with one peek.
+// When the budget ends inside a positive group test the reference still
+// deposits a one at the scan position; so does this.
+struct PlaneBuf {
+  uint64_t* p;
+  int stride;
+};
+
 template <int P, int N, class Source>
-ZG_HD unsigned decode_planes(Source& in, unsigned budget, unsigned maxprec, uint64_t (&pl)[P]) {
+ZG_HD unsigned decode_planes(Source& in, unsigned budget, unsigned maxprec, PlaneBuf pb) {
   const int kmin = (unsigned)P > maxprec ? P - (int)maxprec : 0;
   unsigned bits = budget, n = 0;
-#pragma unroll
-  for (int k = P - 1; k >= 0; k--) {
-    uint64_t x = 0;
-    if (k >= kmin && bits) {
-      const unsigned m = n < bits ? n : bits;
-      x = in.read(m);
-      bits -= m;
-      while (bits && n < (unsigned)N) {
+  int k = P - 1;
+  for (; k >= kmin && bits; k--) {
+    const unsigned m = n < bits ? n : bits;
+    uint64_t x = in.read(m);
+    bits -= m;
+    while (bits && n < (unsigned)N) {
+      // group-test bit plus at most min(bits - 1, N - 1 - n) scan bits
+      unsigned cap = N - 1 - n;
+      if (cap > bits - 1) cap = bits - 1;
+      const uint64_t w = in.peek(cap + 1);
+      if (!(w & 1)) {          // negative test: rest of the plane is zero
+        in.skip(1);
         bits--;
-        if (!in.read(1)) break;
-        unsigned avail = N - 1 - n;
-        if (avail > bits) avail = bits;
-        const uint64_t w = in.peek(avail);
-        unsigned z;
-        if (w) { z = ctz64(w); in.skip(z + 1); bits -= z + 1; }
-        else { z = avail; in.skip(avail); bits -= avail; }
-        n += z;
-        x |= uint64_t(1) << n;
-        n++;
+        break;
       }
+      const uint64_t scan = w >> 1;
+      unsigned z;
+      if (scan) {
+        z = ctz64(scan);
+        in.skip(z + 2);
+        bits -= z + 2;
+      } else {
+        z = cap;
+        in.skip(cap + 1);
+        bits -= cap + 1;
+      }
+      n += z;
+      x |= uint64_t(1) << n;
+      n++;
     }
-    pl[k] = x;
+    pb.p[k * pb.stride] = x;
   }
+  for (; k >= 0; k--) pb.p[k * pb.stride] = 0;
   return budget - bits;
 }
 
@@ -582,7 +609,10 @@ ZG_HD unsigned encode_planes_wide(Sink& out, unsigned budget, unsigned maxprec, 
     uint64_t pl[4] = {0, 0, 0, 0};
     for (int i = 0; i < N; i++) pl[i >> 6] |= (uint64_t)((u[i] >> k) & 1u) << (i & 63);
     const unsigned m = n < bits ? n : bits;
-    for (unsigned i = 0; i < m; i += 64) out.put(pl[i >> 6], m - i < 64 ? m - i : 64);
+    for (unsigned i = 0; i < m; i += 64) {
+      const unsigned c = m - i < 64 ? m - i : 64;
+      out.put(low_bits(pl[i >> 6], c), c);
+    }
     bits -= m;
     while (bits && n < (unsigned)N) {
       bits--;
@@ -640,12 +670,15 @@ ZG_HD unsigned decode_planes_wide(Source& in, unsigned budget, unsigned maxprec,
 
 template <int D, typename I, class Source>
 ZG_HD unsigned uncode_coeffs(Source& in, unsigned budget, unsigned maxprec,
-                             typename std::make_unsigned<I>::type (&u)[1 << (2 * D)]) {
+                             typename std::make_unsigned<I>::type (&u)[1 << (2 * D)], PlaneBuf pb) {
   using U = typename std::make_unsigned<I>::type;
   constexpr int N = 1 << (2 * D);
+  constexpr int P = 8 * sizeof(U);
   if constexpr (N <= 64) {
-    uint64_t pl[8 * sizeof(U)];
-    const unsigned bits = decode_planes<8 * sizeof(U), N>(in, budget, maxprec, pl);
+    const unsigned bits = decode_planes<P, N>(in, budget, maxprec, pb);
+    uint64_t pl[P];
+#pragma unroll
+    for (int k = 0; k < P; k++) pl[k] = pb.p[k * pb.stride];
     take_planes<N>(pl, u);
     return bits;
   } else {
@@ -655,11 +688,11 @@ ZG_HD unsigned uncode_coeffs(Source& in, unsigned budget, unsigned maxprec,
 
 template <int D, typename I, class Source>
 ZG_HD unsigned decode_ints(Source& in, unsigned minbits, unsigned maxbits, unsigned maxprec,
-                           I (&v)[1 << (2 * D)]) {
+                           I (&v)[1 << (2 * D)], PlaneBuf pb) {
   using U = typename std::make_unsigned<I>::type;
   constexpr int N = 1 << (2 * D);
   U u[N];
-  unsigned bits = uncode_coeffs<D, I>(in, maxbits, maxprec, u);
+  unsigned bits = uncode_coeffs<D, I>(in, maxbits, maxprec, u, pb);
   if (bits < minbits) { in.skip_long(minbits - bits); bits = minbits; }
 #pragma unroll (N <= 64 ? N : 1)
   for (int i = 0; i < N; i++) v[perm<D>(i)] = from_nb<I>(u[i]);
@@ -668,13 +701,13 @@ ZG_HD unsigned decode_ints(Source& in, unsigned minbits, unsigned maxbits, unsig
 }
 
 template <int D, typename I, class Source>
-ZG_HD unsigned rev_decode_ints(Source& in, unsigned minbits, unsigned maxbits, I (&v)[1 << (2 * D)]) {
+ZG_HD unsigned rev_decode_ints(Source& in, unsigned minbits, unsigned maxbits, I (&v)[1 << (2 * D)], PlaneBuf pb) {
   using U = typename std::make_unsigned<I>::type;
   constexpr int N = 1 << (2 * D);
   constexpr unsigned kPBits = sizeof(I) == 4 ? 5 : 6;
   const unsigned prec = (unsigned)in.read(kPBits) + 1;
   U u[N];
-  unsigned bits = kPBits + uncode_coeffs<D, I>(in, maxbits - kPBits, prec, u);
+  unsigned bits = kPBits + uncode_coeffs<D, I>(in, maxbits - kPBits, prec, u, pb);
   if (bits < minbits) { in.skip_long(minbits - bits); bits = minbits; }
 #pragma unroll (N <= 64 ? N : 1)
   for (int i = 0; i < N; i++) v[perm<D>(i)] = from_nb<I>(u[i]);
@@ -689,7 +722,7 @@ ZG_HD unsigned umin(unsigned a, unsigned b) { return a < b ? a : b; }
 
 template <typename S, int D, class Source>
 ZG_HD unsigned decode_float_lossy(Source& in, const BlockParams& p,
-                                  typename Traits<S>::Bits (&raw)[1 << (2 * D)]) {
+                                  typename Traits<S>::Bits (&raw)[1 << (2 * D)], PlaneBuf pb) {
   using T = Traits<S>;
   constexpr int N = 1 << (2 * D);
   unsigned bits = 1;
@@ -698,7 +731,7 @@ ZG_HD unsigned decode_float_lossy(Source& in, const BlockParams& p,
     const int emax = (int)in.read(T::kEBits) - T::kEBias;
     const unsigned maxprec = coded_precision(emax, p.maxprec, p.minexp, D);
     typename T::Int v[N];
-    bits += decode_ints<D>(in, p.minbits - umin(bits, p.minbits), p.maxbits - bits, maxprec, v);
+    bits += decode_ints<D>(in, p.minbits - umin(bits, p.minbits), p.maxbits - bits, maxprec, v, pb);
     inv_cast<S, N>(v, raw, emax);
   } else {
 #pragma unroll (N <= 64 ? N : 1)
@@ -710,7 +743,7 @@ ZG_HD unsigned decode_float_lossy(Source& in, const BlockParams& p,
 
 template <typename S, int D, class Source>
 ZG_HD unsigned decode_float_rev(Source& in, const BlockParams& p,
-                                typename Traits<S>::Bits (&raw)[1 << (2 * D)]) {
+                                typename Traits<S>::Bits (&raw)[1 << (2 * D)], PlaneBuf pb) {
   using T = Traits<S>;
   using B = typename T::Bits;
   using I = typename T::Int;
@@ -721,13 +754,13 @@ ZG_HD unsigned decode_float_rev(Source& in, const BlockParams& p,
     I v[N];
     bits++;
     if (in.read(1)) {
-      bits += rev_decode_ints<D>(in, p.minbits - umin(bits, p.minbits), p.maxbits - bits, v);
+      bits += rev_decode_ints<D>(in, p.minbits - umin(bits, p.minbits), p.maxbits - bits, v, pb);
 #pragma unroll (N <= 64 ? N : 1)
       for (int i = 0; i < N; i++) raw[i] = v[i] < 0 ? ((B)v[i] ^ kTc) : (B)v[i];
     } else {
       bits += T::kEBits;
       const int emax = (int)in.read(T::kEBits) - T::kEBias;
-      bits += rev_decode_ints<D>(in, p.minbits - umin(bits, p.minbits), p.maxbits - bits, v);
+      bits += rev_decode_ints<D>(in, p.minbits - umin(bits, p.minbits), p.maxbits - bits, v, pb);
       if (emax != -T::kEBias) inv_cast<S, N>(v, raw, emax);
       else
         for (int i = 0; i < N; i++) raw[i] = 0;
@@ -788,7 +821,7 @@ ZG_HD unsigned rev_precision(const U (&u)[N], unsigned maxprec) {
 // coefficients.  Lossy floating point: src/template/encodef.c:63-90;
 // reversible floating point: revencodef.c:45-80; integers: encode.c:260-280,
 // revencode.c:57-79.
-template <typename S, int D>
+template <typename S, int D, int kSel = kAnyMode>
 ZG_HD void prepare_coeffs(BlockHead& h, const BlockParams& p, const typename Traits<S>::Bits (&raw)[1 << (2 * D)],
                           typename Traits<S>::UInt (&u)[1 << (2 * D)]) {
   using T = Traits<S>;
@@ -796,7 +829,7 @@ ZG_HD void prepare_coeffs(BlockHead& h, const BlockParams& p, const typename Tra
   using I = typename T::Int;
   using U = typename T::UInt;
   constexpr int N = 1 << (2 * D);
-  const bool rev = p.minexp < kMinExp;
+  const bool rev = is_rev<kSel>(p);
   I v[N];
   h.pad_to = p.minbits;
   h.coded = true;
@@ -1038,21 +1071,29 @@ ZG_HD unsigned encode_block(Sink& out, const BlockParams& p, const typename Trai
   }
 }
 
-template <typename S, int D, class Source>
-ZG_HD unsigned decode_block(Source& in, const BlockParams& p, typename Traits<S>::Bits (&raw)[1 << (2 * D)]) {
+template <typename S, int D, int kSel = kAnyMode, class Source>
+ZG_HD unsigned decode_block(Source& in, const BlockParams& p, typename Traits<S>::Bits (&raw)[1 << (2 * D)],
+                            PlaneBuf pb) {
   using T = Traits<S>;
   constexpr int N = 1 << (2 * D);
-  const bool rev = p.minexp < kMinExp;
+  const bool rev = is_rev<kSel>(p);
   if constexpr (T::kFloat) {
-    return rev ? decode_float_rev<S, D>(in, p, raw) : decode_float_lossy<S, D>(in, p, raw);
+    return rev ? decode_float_rev<S, D>(in, p, raw, pb) : decode_float_lossy<S, D>(in, p, raw, pb);
   } else {
     typename T::Int v[N];
-    const unsigned bits = rev ? rev_decode_ints<D>(in, p.minbits, p.maxbits, v)
-                              : decode_ints<D>(in, p.minbits, p.maxbits, p.maxprec, v);
+    const unsigned bits = rev ? rev_decode_ints<D>(in, p.minbits, p.maxbits, v, pb)
+                              : decode_ints<D>(in, p.minbits, p.maxbits, p.maxprec, v, pb);
 #pragma unroll (N <= 64 ? N : 1)
     for (int i = 0; i < N; i++) raw[i] = (typename T::Bits)v[i];
     return bits;
   }
+}
+
+// same, with the planes in a local array
+template <typename S, int D, class Source>
+ZG_HD unsigned decode_block(Source& in, const BlockParams& p, typename Traits<S>::Bits (&raw)[1 << (2 * D)]) {
+  uint64_t plane[8 * sizeof(typename Traits<S>::UInt)];
+  return decode_block<S, D>(in, p, raw, PlaneBuf{plane, 1});
 }
 
 // ---------------------------------------------------------------------------

@@ -174,32 +174,70 @@ bool vector_ok(const FieldInfo& fi, const void* data) {
 // index registry for variable-rate streams
 
 
+// the registry lives for the whole process (never destroyed, so no CUDA
+// call runs from a static destructor at exit)
 static std::mutex g_reg_mu;
-static std::vector<IndexEntry> g_reg;
+static std::vector<IndexEntry>& g_reg = *new std::vector<IndexEntry>();
 static uint64_t g_tick = 0;
 static const size_t kRegistryBytes = 4ull << 30;
 
-static void free_entry(IndexEntry& e) {
-  if (!e.offsets) return;
-  if (cudaFreeAsync(e.offsets, e.stream) != cudaSuccess) {
-    cudaGetLastError();
-    cudaDeviceSynchronize();
-    cudaFree(e.offsets);
-  }
-  e.offsets = nullptr;
+static cudaStream_t free_stream() {
+  static cudaStream_t st = [] {
+    cudaStream_t s = nullptr;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaGetLastError();
+      s = nullptr;
+    }
+    return s;
+  }();
+  return st;
 }
 
-// drop entries of the same buffer whose stream range overlaps [bit0, end)
+DevIndex::~DevIndex() {
+  if (!ptr) return;
+  cudaStream_t fs = free_stream();
+  if (written) {
+    cudaStreamWaitEvent(fs, written, 0);
+    cudaEventDestroy(written);
+  }
+  if (cudaFreeAsync(ptr, fs) != cudaSuccess) cudaGetLastError();
+}
+
+IndexRef make_index(size_t nblocks, cudaStream_t st, cudaError_t& err) {
+  auto idx = std::make_shared<DevIndex>();
+  err = cudaMallocAsync((void**)&idx->ptr, nblocks ? nblocks * 8 : 8, st);
+  if (err != cudaSuccess) {
+    idx->ptr = nullptr;
+    return nullptr;
+  }
+  return idx;
+}
+
+IndexEntry make_entry(const void* begin, uint64_t bit0, uint64_t end_bit, const FieldInfo& fi, const Job& j,
+                      IndexRef index) {
+  IndexEntry e;
+  e.begin = begin;
+  e.bit0 = bit0;
+  e.end_bit = end_bit;
+  e.nblocks = fi.nblocks;
+  e.type = fi.type;
+  e.dims = fi.dims;
+  e.minbits = j.minbits;
+  e.maxbits = j.maxbits;
+  e.maxprec = j.maxprec;
+  e.minexp = j.minexp;
+  e.index = std::move(index);
+  return e;
+}
+
+// drop entries of the same buffer whose stream range overlaps [bit0, end);
+// their memory is released when the last holder lets go
 void registry_invalidate(const void* begin, uint64_t bit0, uint64_t end) {
   std::lock_guard<std::mutex> lk(g_reg_mu);
   for (size_t i = 0; i < g_reg.size();) {
     IndexEntry& e = g_reg[i];
-    if (e.begin == begin && e.bit0 < end && bit0 < e.end_bit) {
-      free_entry(e);
-      g_reg.erase(g_reg.begin() + i);
-    } else {
-      i++;
-    }
+    if (e.begin == begin && e.bit0 < end && bit0 < e.end_bit) g_reg.erase(g_reg.begin() + i);
+    else i++;
   }
 }
 
@@ -212,22 +250,19 @@ void registry_insert(const IndexEntry& ne) {
     auto it = std::min_element(g_reg.begin(), g_reg.end(),
                                [](const IndexEntry& a, const IndexEntry& b) { return a.tick < b.tick; });
     bytes -= it->nblocks * 8;
-    free_entry(*it);
     g_reg.erase(it);
   }
   g_reg.push_back(ne);
   g_reg.back().tick = ++g_tick;
 }
 
-bool registry_find(const void* begin, uint64_t bit0, const FieldInfo& fi, const zfp_stream* z,
-                          cudaStream_t st, IndexEntry& out) {
+bool registry_find(const void* begin, uint64_t bit0, const FieldInfo& fi, const zfp_stream* z, IndexEntry& out) {
   std::lock_guard<std::mutex> lk(g_reg_mu);
   for (auto& e : g_reg)
     if (e.begin == begin && e.bit0 == bit0 && e.nblocks == fi.nblocks && e.type == fi.type &&
         e.dims == fi.dims && e.minbits == z->minbits && e.maxbits == z->maxbits && e.maxprec == z->maxprec &&
         e.minexp == z->minexp) {
       e.tick = ++g_tick;
-      e.stream = st;
       out = e;
       return true;
     }
@@ -391,19 +426,16 @@ size_t gpu_compress(zfp_stream* z, const zfp_field* f) {
   job.bit0 = bit0;
   job.head_word = ss.bits ? (ss.buffer & ((1ull << ss.bits) - 1)) : 0;
 
-  uint64_t* offsets = nullptr;
+  IndexRef index;
   if (!fixed) {
-    if ((e = cudaMallocAsync((void**)&offsets, fi.nblocks * 8, st)) != cudaSuccess)
-      return fail_cuda("zfp_compress: index alloc", e);
-    job.offsets = offsets;
+    index = make_index(fi.nblocks, st, e);
+    if (!index) return fail_cuda("zfp_compress: index alloc", e);
+    job.offsets = index->ptr;
     job.flags |= kWriteIndex;
   }
 
   LaunchMem lm;
-  if ((e = lm.make(job.ntiles, st)) != cudaSuccess) {
-    if (offsets) cudaFreeAsync(offsets, st);
-    return fail_cuda("zfp_compress: scratch", e);
-  }
+  if ((e = lm.make(job.ntiles, st)) != cudaSuccess) return fail_cuda("zfp_compress: scratch", e);
   job.result = lm.result;
 
   LaunchArgs a;
@@ -415,10 +447,8 @@ size_t gpu_compress(zfp_stream* z, const zfp_field* f) {
   DevBuf gimg;
   if ((e = plan_launch(a, fixed ? z->maxbits : bound, job.ntiles, plane_bytes(fi.esize, fi.dims), gimg, st)) !=
           cudaSuccess ||
-      (e = launch_encode_any(fi.type, fi.dims, a, st)) != cudaSuccess) {
-    if (offsets) cudaFreeAsync(offsets, st);
+      (e = launch_encode_any(fi.type, fi.dims, a, st)) != cudaSuccess)
     return fail_cuda("zfp_compress: launch", e);
-  }
 
   if (fixed && field_dev && stream_dev && ep->async) {
     const uint64_t end = bit0 + fi.nblocks * (uint64_t)z->maxbits;
@@ -429,12 +459,9 @@ size_t gpu_compress(zfp_stream* z, const zfp_field* f) {
 
   JobResult res;
   if ((e = cudaMemcpyAsync(&res, lm.result, sizeof res, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-      (e = cudaStreamSynchronize(st)) != cudaSuccess) {
-    if (offsets) cudaFreeAsync(offsets, st);
+      (e = cudaStreamSynchronize(st)) != cudaSuccess)
     return fail_cuda("zfp_compress: kernel", e);
-  }
   if (res.status) {
-    if (offsets) cudaFreeAsync(offsets, st);
     return fail(res.status & kStatusOverflow ? "zfp_compress: stream buffer too small"
                                              : "zfp_compress: GPU wait timed out");
   }
@@ -443,27 +470,11 @@ size_t gpu_compress(zfp_stream* z, const zfp_field* f) {
     const uint64_t w_end = (end + 63) / 64;
     if ((e = cudaMemcpyAsync(ss.begin + w_first, dwords + w_first, (w_end - w_first) * 8, cudaMemcpyDeviceToHost,
                              st)) != cudaSuccess ||
-        (e = cudaStreamSynchronize(st)) != cudaSuccess) {
-      if (offsets) cudaFreeAsync(offsets, st);
+        (e = cudaStreamSynchronize(st)) != cudaSuccess)
       return fail_cuda("zfp_compress: stream download", e);
-    }
   }
-  if (offsets) {
-    IndexEntry ne;
-    ne.begin = ss.begin;
-    ne.bit0 = bit0;
-    ne.end_bit = end;
-    ne.nblocks = fi.nblocks;
-    ne.type = fi.type;
-    ne.dims = fi.dims;
-    ne.minbits = z->minbits;
-    ne.maxbits = z->maxbits;
-    ne.maxprec = z->maxprec;
-    ne.minexp = z->minexp;
-    ne.offsets = offsets;
-    ne.stream = st;
-    ne.tick = 0;
-    registry_insert(ne);
+  if (index) {
+    registry_insert(make_entry(ss.begin, bit0, end, fi, job, index));   // written: the stream was synchronised
   } else {
     registry_invalidate(ss.begin, bit0, end);
   }
@@ -500,7 +511,7 @@ size_t gpu_decompress(zfp_stream* z, zfp_field* f) {
     end = bit0 + fi.nblocks * (uint64_t)z->maxbits;
     if ((end + 63) / 64 > cap_words) return fail("zfp_decompress: stream shorter than the field");
   } else {
-    have_index = registry_find(ss.begin, bit0, fi, z, st, ent);
+    have_index = registry_find(ss.begin, bit0, fi, z, ent);
     if (have_index) end = ent.end_bit;
   }
 
@@ -544,18 +555,18 @@ size_t gpu_decompress(zfp_stream* z, zfp_field* f) {
   if ((e = lm.make(job.ntiles, st)) != cudaSuccess) return fail_cuda("zfp_decompress: scratch", e);
   job.result = lm.result;
 
-  uint64_t* parsed = nullptr;
+  IndexRef parsed;
   auto parse = [&]() -> cudaError_t {
     cudaError_t pe;
-    if (!parsed && (pe = cudaMallocAsync((void**)&parsed, fi.nblocks * 8, st)) != cudaSuccess) return pe;
+    if (!parsed && !(parsed = make_index(fi.nblocks, st, pe))) return pe;
     Job pj = job;
-    pj.offsets = parsed;
+    pj.offsets = parsed->ptr;
     if ((pe = launch_parse_any(fi.type, fi.dims, pj, st)) != cudaSuccess) return pe;
     JobResult r;
     if ((pe = cudaMemcpyAsync(&r, lm.result, sizeof r, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return pe;
     if ((pe = cudaStreamSynchronize(st)) != cudaSuccess) return pe;
     end = r.end_bit;
-    job.offsets = parsed;
+    job.offsets = parsed->ptr;
     job.end_bit = end;
     job.flags &= ~kVerify;
     return cudaSuccess;
@@ -563,11 +574,10 @@ size_t gpu_decompress(zfp_stream* z, zfp_field* f) {
 
   if (!fixed) {
     if (have_index) {
-      job.offsets = ent.offsets;
+      job.offsets = ent.index->ptr;
       job.end_bit = ent.end_bit;
       job.flags |= kVerify;
     } else if ((e = parse()) != cudaSuccess) {
-      if (parsed) cudaFreeAsync(parsed, st);
       return fail_cuda("zfp_decompress: parse", e);
     }
   }
@@ -577,63 +587,35 @@ size_t gpu_decompress(zfp_stream* z, zfp_field* f) {
   a.njobs = 1;
   a.sc = lm.sc;
   DevBuf gimg;
-  if ((e = plan_launch(a, fixed ? z->maxbits : bound, job.ntiles, 0, gimg, st)) != cudaSuccess) {
-    if (parsed) cudaFreeAsync(parsed, st);
+  if ((e = plan_launch(a, fixed ? z->maxbits : bound, job.ntiles, plane_bytes(fi.esize, fi.dims), gimg, st)) !=
+      cudaSuccess)
     return fail_cuda("zfp_decompress: plan", e);
-  }
   a.one = job;
-  if ((e = launch_decode_any(fi.type, fi.dims, a, st)) != cudaSuccess) {
-    if (parsed) cudaFreeAsync(parsed, st);
-    return fail_cuda("zfp_decompress: launch", e);
-  }
+  if ((e = launch_decode_any(fi.type, fi.dims, a, st)) != cudaSuccess) return fail_cuda("zfp_decompress: launch", e);
 
   const bool async_ok = fixed && field_dev && stream_dev && ep->async;
   if (!async_ok) {
     JobResult res;
     if ((e = cudaMemcpyAsync(&res, lm.result, sizeof res, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-        (e = cudaStreamSynchronize(st)) != cudaSuccess) {
-      if (parsed) cudaFreeAsync(parsed, st);
+        (e = cudaStreamSynchronize(st)) != cudaSuccess)
       return fail_cuda("zfp_decompress: kernel", e);
-    }
     if (res.status & kStatusIndex) {
       // the recorded index does not describe this stream: recover and decode again
-      if ((e = cudaMemsetAsync(lm.result, 0, sizeof(JobResult), st)) != cudaSuccess || (e = parse()) != cudaSuccess) {
-        if (parsed) cudaFreeAsync(parsed, st);
+      if ((e = cudaMemsetAsync(lm.result, 0, sizeof(JobResult), st)) != cudaSuccess || (e = parse()) != cudaSuccess)
         return fail_cuda("zfp_decompress: parse", e);
-      }
       a.one = job;
       if ((e = launch_decode_any(fi.type, fi.dims, a, st)) != cudaSuccess ||
-          (e = cudaStreamSynchronize(st)) != cudaSuccess) {
-        if (parsed) cudaFreeAsync(parsed, st);
+          (e = cudaStreamSynchronize(st)) != cudaSuccess)
         return fail_cuda("zfp_decompress: kernel", e);
-      }
     }
   }
   if (!field_dev) {
     char* dst = (char*)f->data + fi.lo * (ptrdiff_t)fi.esize;
     if ((e = cudaMemcpyAsync(dst, fstage.p, span, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-        (e = cudaStreamSynchronize(st)) != cudaSuccess) {
-      if (parsed) cudaFreeAsync(parsed, st);
+        (e = cudaStreamSynchronize(st)) != cudaSuccess)
       return fail_cuda("zfp_decompress: field download", e);
-    }
   }
-  if (parsed) {
-    IndexEntry ne;
-    ne.begin = ss.begin;
-    ne.bit0 = bit0;
-    ne.end_bit = end;
-    ne.nblocks = fi.nblocks;
-    ne.type = fi.type;
-    ne.dims = fi.dims;
-    ne.minbits = z->minbits;
-    ne.maxbits = z->maxbits;
-    ne.maxprec = z->maxprec;
-    ne.minexp = z->minexp;
-    ne.offsets = parsed;
-    ne.stream = st;
-    ne.tick = 0;
-    registry_insert(ne);
-  }
+  if (parsed) registry_insert(make_entry(ss.begin, bit0, end, fi, job, parsed));
   set_stream_flushed(z->stream, end);
   set_error("");
   return (size_t)((end + 63) / 64) * 8;

@@ -6,6 +6,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <memory>
 
 #include "../../include/zfp.h"
 #include "job.h"
@@ -58,21 +59,36 @@ struct DevBuf {
   ~DevBuf() { release(); }
 };
 
+// A per-block index (start bit of every block) in device memory, shared by
+// the registry and by every launch that reads it.  The last holder to drop
+// it frees it on a library-owned stream, after `written` (an event recorded
+// behind writes that may still be in flight).  Holders keep their reference
+// until the GPU work that reads the index has finished.
+struct DevIndex {
+  uint64_t* ptr = nullptr;
+  cudaEvent_t written = nullptr;
+  ~DevIndex();
+};
+using IndexRef = std::shared_ptr<DevIndex>;
+
+// allocate an index for nblocks blocks (stream-ordered on st)
+IndexRef make_index(size_t nblocks, cudaStream_t st, cudaError_t& err);
+
 struct IndexEntry {
-  const void* begin;
-  uint64_t bit0, end_bit, nblocks;
-  int type, dims;
-  uint32_t minbits, maxbits, maxprec;
-  int32_t minexp;
-  uint64_t* offsets;       // device, nblocks words
-  cudaStream_t stream;     // last stream that used it (frees are ordered after it)
-  uint64_t tick;
+  const void* begin = nullptr;
+  uint64_t bit0 = 0, end_bit = 0, nblocks = 0;
+  int type = 0, dims = 0;
+  uint32_t minbits = 0, maxbits = 0, maxprec = 0;
+  int32_t minexp = 0;
+  IndexRef index;
+  uint64_t tick = 0;
 };
 
+IndexEntry make_entry(const void* begin, uint64_t bit0, uint64_t end_bit, const FieldInfo& fi, const Job& j,
+                      IndexRef index);
 void registry_invalidate(const void* begin, uint64_t bit0, uint64_t end);
 void registry_insert(const IndexEntry& ne);
-bool registry_find(const void* begin, uint64_t bit0, const FieldInfo& fi, const zfp_stream* z, cudaStream_t st,
-                   IndexEntry& out);
+bool registry_find(const void* begin, uint64_t bit0, const FieldInfo& fi, const zfp_stream* z, IndexEntry& out);
 
 cudaError_t launch_encode_any(int type, int dims, const LaunchArgs& a, cudaStream_t st);
 cudaError_t launch_decode_any(int type, int dims, const LaunchArgs& a, cudaStream_t st);

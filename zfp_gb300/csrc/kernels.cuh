@@ -97,8 +97,11 @@ __device__ __forceinline__ void gather(const Job& job, uint64_t b, B (&raw)[1 <<
           for (int x = 0; x < EX; x++)
             raw[x + 4 * y + 16 * z + 64 * w] = __ldg(base + x * s0 + y * s1 + z * s2 + w * s3);
   } else {
+#pragma unroll (N <= 64 ? EW : 1)
     for (int w = 0; w < EW; w++)
+#pragma unroll (N <= 64 ? EZ : 1)
       for (int z = 0; z < EZ; z++)
+#pragma unroll (N <= 64 ? EY : 1)
         for (int y = 0; y < EY; y++)
 #pragma unroll
           for (int x = 0; x < EX; x++)
@@ -148,11 +151,17 @@ __device__ __forceinline__ void scatter(const Job& job, uint64_t b, const B (&ra
           for (int x = 0; x < EX; x++)
             base[x * s0 + y * s1 + z * s2 + w * s3] = raw[x + 4 * y + 16 * z + 64 * w];
   } else {
-    for (int w = 0; w < cnt[3]; w++)
-      for (int z = 0; z < cnt[2]; z++)
-        for (int y = 0; y < cnt[1]; y++)
-          for (int x = 0; x < cnt[0]; x++)
-            base[x * s0 + y * s1 + z * s2 + w * s3] = raw[x + 4 * y + 16 * z + 64 * w];
+    // fixed trip counts with predicated stores keep raw[] in registers
+#pragma unroll (N <= 64 ? EW : 1)
+    for (int w = 0; w < EW; w++)
+#pragma unroll (N <= 64 ? EZ : 1)
+      for (int z = 0; z < EZ; z++)
+#pragma unroll (N <= 64 ? EY : 1)
+        for (int y = 0; y < EY; y++)
+#pragma unroll
+          for (int x = 0; x < EX; x++)
+            if (x < cnt[0] && y < cnt[1] && z < cnt[2] && w < cnt[3])
+              base[x * s0 + y * s1 + z * s2 + w * s3] = raw[x + 4 * y + 16 * z + 64 * w];
   }
 }
 
@@ -338,7 +347,7 @@ __device__ __forceinline__ void write_tile(const Job& job, const LaunchScratch& 
 // ---------------------------------------------------------------------------
 // encode one tile
 
-template <typename S, int D>
+template <typename S, int D, int kSel>
 __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch& sc, uint32_t gt, uint64_t* img,
                                             uint32_t img_words, uint64_t* planes) {
   using B = typename Traits<S>::Bits;
@@ -362,11 +371,11 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
     gather<B, D>(job, b, raw);
     if constexpr (N <= 64) {
       U u[N];
-      prepare_coeffs<S, D>(h, p, raw, u);
+      prepare_coeffs<S, D, kSel>(h, p, raw, u);
       if (h.coded) store_planes<N>(u, my_planes, kTile);
       len = fixed ? job.maxbits : block_bits<P, N>(h, my_planes, kTile);
     } else {
-      prepare_coeffs<S, D>(wc.h, p, raw, wc.u);
+      prepare_coeffs<S, D, kSel>(wc.h, p, raw, wc.u);
       len = fixed ? job.maxbits : wc.length();
     }
   }
@@ -405,8 +414,9 @@ constexpr size_t plane_smem_bytes() {
 // ---------------------------------------------------------------------------
 // decode one tile
 
-template <typename S, int D>
-__device__ __forceinline__ void decode_tile(const Job& job, uint32_t gt, uint64_t* img, uint32_t img_words) {
+template <typename S, int D, int kSel>
+__device__ __forceinline__ void decode_tile(const Job& job, uint32_t gt, uint64_t* img, uint32_t img_words,
+                                            uint64_t* planes) {
   using B = typename Traits<S>::Bits;
   constexpr int N = 1 << (2 * D);
   const uint32_t lt = gt - job.tile0;
@@ -440,6 +450,7 @@ __device__ __forceinline__ void decode_tile(const Job& job, uint32_t gt, uint64_
   if (!active) return;
 
   const BlockParams p{job.minbits, job.maxbits, job.maxprec, job.minexp};
+  const PlaneBuf pb{planes + threadIdx.x, kTile};
   B raw[N];
   uint64_t end;
   if (staged) {
@@ -447,14 +458,14 @@ __device__ __forceinline__ void decode_tile(const Job& job, uint32_t gt, uint64_
     in.base = img;
     in.cap = nwords;
     in.seek(start - (w0 << 6));
-    decode_block<S, D>(in, p, raw);
+    decode_block<S, D, kSel>(in, p, raw, pb);
     end = in.at + (w0 << 6);
   } else {
     WordSource in;
     in.base = job.words;
     in.cap = job.cap_words;
     in.seek(start);
-    decode_block<S, D>(in, p, raw);
+    decode_block<S, D, kSel>(in, p, raw, pb);
     end = in.at;
   }
   if ((job.flags & kVerify) && end != expect) atomicOr(&job.result->status, (unsigned)kStatusIndex);
@@ -482,7 +493,7 @@ __device__ __forceinline__ const Job* resolve_job(const Job& one, const Job* job
   return s_job;
 }
 
-template <typename S, int D, bool kMulti>
+template <typename S, int D, bool kMulti, int kSel>
 __global__ void __launch_bounds__(kTile) encode_kernel(const __grid_constant__ Job one, const Job* jobs, int njobs,
                                                        LaunchScratch sc, uint32_t total_tiles, int use_ticket,
                                                        uint64_t* gimg, uint32_t img_words) {
@@ -497,20 +508,21 @@ __global__ void __launch_bounds__(kTile) encode_kernel(const __grid_constant__ J
     const uint32_t gt = s_tile;
     if (gt >= total_tiles) break;
     const Job* job = resolve_job<kMulti>(one, jobs, njobs, gt, &s_job);
-    encode_tile<S, D>(*job, sc, gt, img, img_words, planes);
+    encode_tile<S, D, kSel>(*job, sc, gt, img, img_words, planes);
     __syncthreads();
   }
 }
 
-template <typename S, int D, bool kMulti>
+template <typename S, int D, bool kMulti, int kSel>
 __global__ void __launch_bounds__(kTile) decode_kernel(const __grid_constant__ Job one, const Job* jobs, int njobs,
                                                        uint32_t total_tiles, uint64_t* gimg, uint32_t img_words) {
   extern __shared__ uint64_t smem_img[];
   uint64_t* img = gimg ? gimg + (size_t)blockIdx.x * img_words : smem_img;
+  uint64_t* planes = smem_img + (gimg ? 0 : img_words);
   __shared__ Job s_job;
   for (uint32_t gt = blockIdx.x; gt < total_tiles; gt += gridDim.x) {
     const Job* job = resolve_job<kMulti>(one, jobs, njobs, gt, &s_job);
-    decode_tile<S, D>(*job, gt, img, img_words);
+    decode_tile<S, D, kSel>(*job, gt, img, img_words, planes);
     __syncthreads();
   }
 }

@@ -26,9 +26,8 @@ template <typename S, int D> cudaError_t run_encode(const LaunchArgs& a, cudaStr
 template <typename S, int D> cudaError_t run_decode(const LaunchArgs& a, cudaStream_t st);
 template <typename S, int D> cudaError_t run_parse(const Job& job, cudaStream_t st);
 
-// dynamic shared memory a kernel may request (GB300: 227 KB per CTA)
-constexpr size_t kSmemLimit = 227 * 1024;
-// a tile image plus bit planes larger than this is staged in global memory instead
+// a tile image plus bit planes larger than this is staged in global memory
+// instead (GB300 allows 227 KB of shared memory per CTA, static included)
 constexpr size_t kMaxTileSmem = 216 * 1024;
 
 // shared memory the encoder keeps for bit planes: 1-3D blocks only
