@@ -671,15 +671,18 @@ def e2e_run(lib, torch, codec, fields, args):
         hosts.append((fd, hx, hout, hbuf))
     h2d = d2h = 0
     sizes = {}
+    staged = [0]
 
     def step():
-        nonlocal h2d, d2h
+        staged[0] = 0
         for fd, hx, hout, hbuf in hosts:
             for mode, arg in MODES:
                 r = codec.run("c", hx.data_ptr(), fd["ztype"], fd["n"], mode, arg, hbuf.data_ptr(), fd["cap"],
                               async_=False)
+                staged[0] += lib.zfp_gb300_last_staged_bytes()
                 r2 = codec.run("d", hout.data_ptr(), fd["ztype"], fd["n"], mode, arg, hbuf.data_ptr(), fd["cap"],
                                async_=False)
+                staged[0] += lib.zfp_gb300_last_staged_bytes()
                 if not r or r2 != r:
                     raise RuntimeError(f"e2e {fd['name']} {mode} failed")
                 sizes[(fd["name"], mode)] = r
@@ -699,7 +702,9 @@ def e2e_run(lib, torch, codec, fields, args):
             d2h += fd["raw"] + sizes[(fd["name"], mode)]
     _, world, _ = dist_info()
     return {"value": round(world * raw_step * n / dt / 1e9, 2), "unit": "GB/s", "h2d_bytes_per_step": h2d,
-            "d2h_bytes_per_step": d2h, "steps": n, "buffers": "pinned host field and stream"}
+            "d2h_bytes_per_step": d2h, "steps": n,
+            "buffers": "pinned host field and stream, read and written in place by the kernels over the host link "
+                       "(h2d/d2h = bytes crossing it)", "staged_bytes_per_step": staged[0]}
 
 
 # ---------------------------------------------------------------------------

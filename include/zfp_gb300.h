@@ -33,6 +33,13 @@ zfp_bool zfp_gb300_stream_synchronize(zfp_stream* zfp);
 /* Reason for the last failure (return value 0) seen by this thread, or "". */
 const char* zfp_gb300_last_error(void);
 
+/* Bytes copied between host and device memory by this thread's last
+ * zfp_compress / zfp_decompress.  Device buffers, and page-locked host
+ * buffers mapped into the device (cudaHostAlloc, cudaHostRegister), are
+ * read and written in place by the kernels, so they cost no copy; other
+ * host buffers are staged through device memory. */
+size_t zfp_gb300_last_staged_bytes(void);
+
 /* ---- batches: many fields in one launch --------------------------------
  * A batch codes `count` independent fields, each with its own zfp_stream
  * (mode, parameters and bit stream, positioned where that stream's next

@@ -31,6 +31,29 @@ struct VecSink {
   ZG_HD void pad(unsigned n) { pos += n; }
 };
 
+// Position-addressed sink for zg::emit_block_or: ORs v (n bits, clean) at
+// bit start + pos.  Writes at or past `end` (the block's returned length,
+// checked after the block) are recorded as overruns.
+static bool g_or_overrun = false;
+static int g_coder = 0;   // 0: emit_block (sequential puts), 1: emit_block_or
+
+struct OrSink {
+  uint64_t* words;
+  uint64_t start;
+  uint64_t hi = 0;        // one past the highest bit written
+  ZG_HD void set(uint64_t pos, uint64_t v, unsigned n) {
+#if !defined(__CUDA_ARCH__)
+    if (n < 64 && (v >> n)) g_unclean_put = true;
+#endif
+    if (!n) return;
+    const uint64_t a = start + pos;
+    const unsigned o = (unsigned)(a & 63);
+    words[a >> 6] |= v << o;
+    if (o && o + n > 64) words[(a >> 6) + 1] |= v >> (64 - o);
+    if (pos + n > hi) hi = pos + n;
+  }
+};
+
 struct Geom {
   int dims;
   size_t n[4], nb[4];
@@ -86,6 +109,23 @@ uint64_t compress_t(const Geom& g, const zg::BlockParams& p, const void* data, u
     B raw[1 << (2 * D)];
     size_t org[4], cnt[4];
     gather<B, D>(g, (const B*)data, b, raw, org, cnt);
+    if constexpr ((1 << (2 * D)) <= 64) {
+      if (g_coder == 1) {
+        using U = typename zg::Traits<S>::UInt;
+        constexpr int N = 1 << (2 * D), P = 8 * sizeof(U);
+        zg::BlockHead h;
+        U u[N];
+        uint64_t plane[P];
+        uint16_t base[P];
+        zg::prepare_coeffs<S, D>(h, p, raw, u);
+        if (h.coded) zg::store_planes<N>(u, plane, 1);
+        OrSink os{words, out.pos};
+        const unsigned bits = zg::emit_block_or<P, N>(os, h, plane, 1, base, 1);
+        if (os.hi > bits) g_or_overrun = true;
+        out.pos += bits;
+        continue;
+      }
+    }
     zg::encode_block<S, D>(out, p, raw);
   }
   return out.pos;
@@ -144,6 +184,14 @@ uint64_t decompress_s(const Geom& g, const zg::BlockParams& p, void* d, const ui
 
 }  // namespace
 
+extern "C" void zgh_set_coder(int c) { g_coder = c; }
+
+extern "C" int zgh_or_overrun(void) {
+  const int r = g_or_overrun;
+  g_or_overrun = false;
+  return r;
+}
+
 extern "C" int zgh_unclean_put(void) {
   const int r = g_unclean_put;
   g_unclean_put = false;
@@ -172,4 +220,23 @@ extern "C" uint64_t zgh_decompress(int type, int dims, const size_t* n, const pt
     case 3: return decompress_s<float>(g, p, data, words, cap, bit0);
     default: return decompress_s<double>(g, p, data, words, cap, bit0);
   }
+}
+
+// the integer casts against the hardware multiply they replace:
+// out[i] = bits of (double)v[i] * 2^e, trunc[i] = trunc(x[i] * 2^se)
+extern "C" void zgh_int_scale(const int64_t* v, size_t n, int e, uint64_t* out) {
+  for (size_t i = 0; i < n; i++) out[i] = zg::int_scale<double>(v[i], e);
+}
+extern "C" void zgh_scale_trunc(const uint64_t* x, size_t n, int se, int64_t* out) {
+  for (size_t i = 0; i < n; i++) out[i] = zg::scale_trunc<double>(x[i], se);
+}
+extern "C" int zgh_bfp_exact64(const uint64_t* raw, int emax, int special) {
+  uint64_t b[64];
+  for (int i = 0; i < 64; i++) b[i] = raw[i];
+  return zg::bfp_exact<double, 64>(b, emax, special != 0);
+}
+extern "C" int zgh_bfp_exact32(const uint32_t* raw, int emax, int special) {
+  uint32_t b[64];
+  for (int i = 0; i < 64; i++) b[i] = raw[i];
+  return zg::bfp_exact<float, 64>(b, emax, special != 0);
 }

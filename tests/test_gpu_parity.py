@@ -265,3 +265,42 @@ def test_errors_return_zero(lib, cuda):
     r, pos = zfp_run(lib, "compress", b.ctypes.data, 3, n, s, "reversible", None, buf.ctypes.data, 16 * 8)
     assert r == 0 and pos == 0
     assert "small" in lib.zfp_gb300_last_error().decode()
+
+
+def test_pinned_host_buffers_zero_copy(lib, oracle, cuda):
+    """Page-locked host fields and streams are read and written in place by
+    the kernels (nothing is staged through device memory) with the same bits
+    as the oracle; pageable host buffers are still staged."""
+    torch = cuda
+    tdt = {np.float32: torch.float32, np.float64: torch.float64, np.int32: torch.int32, np.int64: torch.int64}
+    cases = [(np.float32, (37, 45, 66), "rate", 8), (np.float64, (21, 30, 47), "accuracy", 1e-4),
+             (np.int32, (300, 301), "precision", 20), (np.float32, (40, 64, 90), "reversible", None),
+             (np.int64, (9, 10, 11, 12), "rate", 12)]
+    for dtype, shape, mode, arg in cases:
+        vals = make_values(dtype, shape)
+        exp_words, _, prm = oracle_stream(oracle, vals, mode, arg)
+        nwords = len(exp_words) + 16
+        hx = torch.empty(shape, dtype=tdt[dtype], pin_memory=True)
+        hx.numpy()[...] = vals
+        hs = torch.zeros(nwords + 8, dtype=torch.int64, pin_memory=True)
+        sptr = hs.data_ptr() + 64            # the stream starts inside the pinned block
+        n, s = geometry(vals)
+        zt = ztype_of(vals)
+        msg = f"{np.dtype(dtype).name} {shape} {mode}={arg}"
+        r, _ = zfp_run(lib, "compress", hx.data_ptr(), zt, n, s, mode, arg, sptr, nwords * 8)
+        assert r == len(exp_words) * 8, (msg, lib.zfp_gb300_last_error())
+        assert lib.zfp_gb300_last_staged_bytes() == 0, msg
+        assert np.array_equal(hs.numpy().view(np.uint64)[8: 8 + len(exp_words)], exp_words), msg
+        hout = torch.zeros(shape, dtype=tdt[dtype], pin_memory=True)
+        r2, _ = zfp_run(lib, "decompress", hout.data_ptr(), zt, n, s, mode, arg, sptr, nwords * 8)
+        assert r2 == r and lib.zfp_gb300_last_staged_bytes() == 0, msg
+        ref_out = np.zeros(shape, dtype=dtype)
+        oracle.decompress(exp_words, ref_out, prm, 0)
+        assert np.array_equal(hout.numpy().view(np.uint8), ref_out.view(np.uint8)), msg
+        # the same stream from pageable memory goes through staging
+        page = np.zeros(nwords, dtype=np.uint64)
+        page[: len(exp_words)] = exp_words
+        out2 = np.zeros(shape, dtype=dtype)
+        r3, _ = zfp_run(lib, "decompress", out2.ctypes.data, zt, n, s, mode, arg, page.ctypes.data, nwords * 8)
+        assert r3 == r and lib.zfp_gb300_last_staged_bytes() > 0, msg
+        assert np.array_equal(out2.view(np.uint8), ref_out.view(np.uint8)), msg

@@ -63,9 +63,14 @@ SPECIAL = {np.float32: np.array([0.0, -0.0, 1e-45, -1e-45, 1e-40, 3.4e38, -3.4e3
                                  1.0, -2.5, 1e-300, 1e-290])}
 
 
+@pytest.mark.parametrize("coder", ["sequential", "positional"])
 @pytest.mark.parametrize("dims", [1, 2, 3, 4])
 @pytest.mark.parametrize("dtype", [np.float32, np.float64, np.int32, np.int64], ids=lambda d: np.dtype(d).name)
-def test_device_codec_on_host_matches_oracle(host, oracle, dims, dtype):
+def test_device_codec_on_host_matches_oracle(host, oracle, dims, dtype, coder):
+    """Both plane coders of codec.cuh: emit_block (sequential puts) and
+    emit_block_or (bits OR-ed at computed positions, used by the encoder
+    kernel for 1-3D blocks)."""
+    host.zgh_set_coder(1 if coder == "positional" else 0)
     rng = np.random.default_rng(dims * 10 + ZTYPE[np.dtype(dtype)])
     modes = [("rate", 4), ("rate", 12.5), ("rate", 1), ("precision", 7), ("precision", 20), ("accuracy", 1e-3),
              ("accuracy", 1e-9), ("reversible", None), ("rate", 32), ("precision", 64), ("expert", (30, 70, 33, -5))]
@@ -90,8 +95,71 @@ def test_device_codec_on_host_matches_oracle(host, oracle, dims, dtype):
             nw = (e0 + 63) // 64
             assert e0 == e1 and np.array_equal(w0[:nw], w1[:nw]), (mode, arg, shape, trial)
             assert not host.zgh_unclean_put(), ("a sink received bits above its length", mode, arg, shape)
+            assert not host.zgh_or_overrun(), ("bits written past the block's length", mode, arg, shape)
             d0 = np.zeros(view.shape, dtype=dtype)
             d1 = np.zeros(view.shape, dtype=dtype)
             x0 = oracle.decompress(w0[: nw + 2], d0, prm, bit0)
             x1 = host_decompress(host, w0[: nw + 2].copy(), d1, prm, bit0)
             assert x0 == x1 and np.array_equal(d0.view(np.uint8), d1.view(np.uint8)), (mode, arg, shape, trial)
+
+
+def test_integer_casts_match_fp64_arithmetic(host):
+    """int_scale / scale_trunc (the double-precision casts done on integer
+    pipes) against numpy's IEEE multiply, over their whole valid range."""
+    rng = np.random.default_rng(11)
+    host.zgh_int_scale.argtypes = [C.c_void_p, C.c_size_t, C.c_int, C.c_void_p]
+    host.zgh_scale_trunc.argtypes = [C.c_void_p, C.c_size_t, C.c_int, C.c_void_p]
+    n = 20000
+    for e in [-1022, -1000, -500, -62, -1, 0, 7, 500, 960]:
+        bits = rng.integers(0, 64, size=n)
+        v = (rng.integers(0, 2**62, size=n, dtype=np.int64) >> (62 - np.minimum(bits, 62))).astype(np.int64)
+        v = np.where(rng.random(n) < 0.5, -v, v)
+        v[:8] = [0, 1, -1, 2**53 + 1, -(2**53 + 3), 2**62 + 1023, -(2**63), 2**63 - 1]
+        out = np.zeros(n, dtype=np.uint64)
+        host.zgh_int_scale(v.ctypes.data, n, e, out.ctypes.data)
+        want = (v.astype(np.float64) * np.ldexp(1.0, e)).view(np.uint64)
+        assert np.array_equal(out, want), e
+    for emax in [-960, -900, -1, 0, 1, 100, 1023, 1024]:
+        se = 62 - emax
+        with np.errstate(over="ignore"):
+            x = np.ldexp(rng.uniform(-1, 1, size=n), emax)
+            x[:6] = [0.0, -0.0, np.ldexp(1.0, emax - 1), -np.ldexp(0.75, emax), 5e-324, -2.2e-308]
+            x = np.where(np.abs(x) < np.ldexp(1.0, emax), x, 0.0)
+        out = np.zeros(n, dtype=np.int64)
+        host.zgh_scale_trunc(x.ctypes.data, n, se, out.ctypes.data)
+        with np.errstate(over="ignore"):
+            want = np.trunc(x * np.ldexp(1.0, se)).astype(np.int64)
+        assert np.array_equal(out, want), emax
+
+
+def test_bfp_exactness_shortcut(host):
+    """bfp_exact's integer test agrees with casting each value and back."""
+    rng = np.random.default_rng(12)
+    host.zgh_bfp_exact64.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    host.zgh_bfp_exact32.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    for dtype, fn, P, I in [(np.float64, host.zgh_bfp_exact64, 64, np.int64),
+                            (np.float32, host.zgh_bfp_exact32, 32, np.int32)]:
+        seen = set()
+        for trial in range(3000):
+            emax = int(rng.integers(-1000 if dtype == np.float64 else -140, 60))
+            k = int(rng.integers(0, P + 4))
+            vals = np.ldexp(np.floor(rng.uniform(-1, 1, 64) * 2.0 ** k), emax - k).astype(dtype)
+            if trial % 5 == 0:
+                vals[rng.integers(0, 64)] = -0.0
+            vals[0] = np.ldexp(0.5, emax) if trial % 3 else vals[0]
+            vals = np.where(np.abs(vals) < np.ldexp(1.0, emax), vals, 0).astype(dtype)
+            if not vals.any():
+                continue
+            em = int(np.max(np.frexp(vals.astype(np.float64))[1]))
+            raw = vals.view(np.uint64 if dtype == np.float64 else np.uint32).copy()
+            with np.errstate(over="ignore", under="ignore", invalid="ignore"):
+                s = np.ldexp(dtype(1), P - 2 - em) if P - 2 - em <= (1023 if P == 64 else 127) else dtype(np.inf)
+                prod = (vals * s).astype(dtype)
+                ok = np.abs(prod) < 2.0 ** (P - 1)
+                iv = np.where(ok, np.trunc(np.where(ok, prod, 0)), -(2.0 ** (P - 1))).astype(I)
+                back = (iv.astype(dtype) * dtype(np.ldexp(1.0, em - (P - 2)))).astype(dtype)
+            want = bool(np.array_equal(back.view(raw.dtype), raw))
+            got = bool(fn(raw.ctypes.data, em, 0))
+            assert got == want, (dtype, em, trial)
+            seen.add(want)
+        assert seen == {True, False}

@@ -21,6 +21,7 @@ _EXT = [
     ("zfp_gb300_stream_set_async", C.c_int, [capi.PZ, C.c_int]),
     ("zfp_gb300_stream_synchronize", C.c_int, [capi.PZ]),
     ("zfp_gb300_last_error", C.c_char_p, []),
+    ("zfp_gb300_last_staged_bytes", C.c_size_t, []),
 ]
 
 _lib = None

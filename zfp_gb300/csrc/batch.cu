@@ -27,13 +27,14 @@ struct BatchGroup {
   int type = 0, dims = 0;
   std::vector<size_t> members;
   uint32_t total_tiles = 0;
-  uint32_t img_words = 0;
+  uint32_t tile_words = 0;     // largest tile image of any member
+  uint32_t img_words = 0;      // shared-memory part (see plan_launch in gpu_codec.cu)
   bool needs_ticket = false;
   Job* d_jobs = nullptr;       // device copy of this group's jobs (sorted by tile0)
   LaunchScratch sc{};
   void* scratch = nullptr;     // zeroed before every launch
   size_t scratch_bytes = 0;
-  uint64_t* gimg = nullptr;    // global staging when a tile image exceeds shared memory
+  uint64_t* gimg = nullptr;    // encode: global slots for tiles larger than img_words
   size_t gimg_words = 0;
 };
 
@@ -80,7 +81,8 @@ static cudaError_t enqueue(zfp_gb300_batch* b, cudaStream_t st, int ctas_per_sm)
     a.grid = (int)std::min<uint64_t>(g.total_tiles, (uint64_t)grid);
     if (g.gimg) {
       a.gimg = g.gimg;
-      a.grid = (int)std::min<uint64_t>((uint64_t)a.grid, g.gimg_words / g.img_words);
+      a.slot_words = g.tile_words;
+      a.grid = (int)std::min<uint64_t>((uint64_t)a.grid, g.gimg_words / g.tile_words);
     }
     e = b->direction == 0 ? launch_encode_any(g.type, g.dims, a, st) : launch_decode_any(g.type, g.dims, a, st);
     if (e != cudaSuccess) return e;
@@ -219,7 +221,7 @@ zfp_gb300_batch* zfp_gb300_batch_create(zfp_stream* const* streams, const zfp_fi
     b->jobs[i].tile0 = g.total_tiles;
     g.total_tiles += b->jobs[i].ntiles;
     const uint64_t bound = fixed ? (uint64_t)z->maxbits : block_bound(fi, z);
-    g.img_words = std::max<uint32_t>(g.img_words, (uint32_t)((uint64_t)kTile * bound / 64 + 4));
+    g.tile_words = std::max<uint32_t>(g.tile_words, (uint32_t)((uint64_t)kTile * bound / 64 + 4));
     g.members.push_back(i);
   }
   if (offset_words) {
@@ -248,9 +250,13 @@ zfp_gb300_batch* zfp_gb300_batch_create(zfp_stream* const* streams, const zfp_fi
     g.sc.tile_state = (unsigned long long*)(p + 64);
     g.sc.side = (unsigned long long*)(p + 64 + t * 8);
     g.sc.side_cnt = (unsigned int*)(p + 64 + t * 24);
-    const size_t extra = plane_bytes(b->info[g.members[0]].esize, g.dims);
-    if ((size_t)g.img_words * 8 + extra > kMaxTileSmem) {
-      g.gimg_words = (size_t)persistent_grid() * 2 * g.img_words;
+    LaunchArgs probe;
+    std::memset(&probe, 0, sizeof probe);
+    probe.jobs = g.d_jobs;
+    const uint32_t room = stage_room_any(g.type, g.dims, probe, b->direction == 0);
+    g.img_words = std::min(g.tile_words, room);
+    if (b->direction == 0 && g.tile_words > room) {
+      g.gimg_words = (size_t)persistent_grid() * 2 * g.tile_words;
       if ((e = cudaMalloc((void**)&g.gimg, g.gimg_words * 8)) != cudaSuccess) {
         fail_cuda("zfp_gb300_batch_create: staging", e);
         destroy(b);

@@ -269,10 +269,23 @@ ZG_HD int block_emax(const typename Traits<S>::Bits (&raw)[N], bool& special) {
   constexpr B kAbs = ~(B(1) << (8 * sizeof(B) - 1));
   constexpr B kInf = B((B(1) << T::kEBits) - 1) << T::kMant;
   B top = 0;
+  if constexpr (sizeof(B) == 8) {
+    // the exponent sits in the high word: 32-bit maxima, plus an OR of the
+    // low words to tell subnormals from zeros
+    uint32_t hi = 0, lo = 0;
 #pragma unroll (N <= 64 ? N : 1)
-  for (int i = 0; i < N; i++) {
-    B a = raw[i] & kAbs;
-    top = a > top ? a : top;
+    for (int i = 0; i < N; i++) {
+      const uint32_t a = (uint32_t)(raw[i] >> 32) & 0x7fffffffu;
+      hi = a > hi ? a : hi;
+      lo |= (uint32_t)raw[i];
+    }
+    top = ((B)hi << 32) | (hi ? 0u : lo);   // same exponent field and zero test as the true maximum
+  } else {
+#pragma unroll (N <= 64 ? N : 1)
+    for (int i = 0; i < N; i++) {
+      B a = raw[i] & kAbs;
+      top = a > top ? a : top;
+    }
   }
   special = top >= kInf;
   if (special) {
@@ -288,26 +301,82 @@ ZG_HD int block_emax(const typename Traits<S>::Bits (&raw)[N], bool& special) {
   return biased ? biased - (T::kEBias - 1) : 1 - T::kEBias;
 }
 
+// |x| = m * 2^q for a finite bit pattern (m = 0 for both zeros)
+template <typename S>
+ZG_HD typename Traits<S>::Bits significand(typename Traits<S>::Bits b, int& q) {
+  using T = Traits<S>;
+  using B = typename T::Bits;
+  const int e = (int)((b >> T::kMant) & ((B(1) << T::kEBits) - 1));
+  q = (e ? e : 1) - (T::kEBias + T::kMant);
+  const B m = b & ((B(1) << T::kMant) - 1);
+  return e ? m | (B(1) << T::kMant) : m;
+}
+
+// trunc(x * 2^se) from the bits alone, for finite x with |x| * 2^se below
+// 2^(P-1).  Equal to the rounded product followed by truncation: scaling by
+// a power of two is exact unless the product falls below the normal range,
+// and such a product truncates to 0 either way.  Double precision uses it
+// because the FP64 pipe of this GPU is narrow.
+template <typename S>
+ZG_HD typename Traits<S>::Int scale_trunc(typename Traits<S>::Bits b, int se) {
+  using T = Traits<S>;
+  using B = typename T::Bits;
+  constexpr int W = 8 * sizeof(B);
+  int q;
+  const B m = significand<S>(b, q);
+  const int t = q + se;
+  const B a = t >= 0 ? B(m << t) : (-t < W ? B(m >> -t) : B(0));
+  const B neg = B(0) - (b >> (W - 1));   // all ones for negative x
+  return (typename T::Int)((a ^ neg) - neg);
+}
+
+// bits of (S)v * 2^e with round-to-nearest-even at the conversion, for
+// results in the normal range (the product itself is then exact)
+template <typename S>
+ZG_HD typename Traits<S>::Bits int_scale(typename Traits<S>::Int v, int e) {
+  using T = Traits<S>;
+  using B = typename T::Bits;
+  constexpr int W = 8 * sizeof(B);
+  constexpr int kDrop = W - 1 - T::kMant;
+  const B neg = B(0) - B(v < 0);
+  const B a = (B(v) ^ neg) - neg;
+  if (!a) return 0;
+  const int lz = clz64((uint64_t)a) - (64 - W);
+  const B n = a << lz;
+  B mant = n >> kDrop;                                   // with the leading one at bit kMant
+  const B rem = n & ((B(1) << kDrop) - 1), half = B(1) << (kDrop - 1);
+  mant += B((rem > half) | ((rem == half) & (unsigned)(mant & 1)));   // a carry lands in the exponent
+  const int ex = W - 1 - lz + e;                         // exponent of the leading one
+  return (B(ex + T::kEBias - 1) << T::kMant) + mant + (neg & (B(1) << (W - 1)));
+}
+
 // block-floating-point cast (src/template/encodef.c:44-59).  Out-of-range
 // or NaN products give the x86 integer-indefinite value, as the reference
 // does on x86-64; that only happens in blocks with NaN/inf or with a scale
 // factor that overflows (tiny blocks), so the common path has no checks.
+template <typename S>
+ZG_HD typename Traits<S>::Int cast_slow(typename Traits<S>::Bits b, S s) {
+  using T = Traits<S>;
+  using I = typename T::Int;
+  const S lim = pow2<S>(T::kPrec - 1);
+  const S x = fmul<S>(s, from_bits<S>(b));
+  return (x < lim && x > -lim) ? trunc_int<S>(x) : (I)((typename T::UInt)1 << (T::kPrec - 1));
+}
+
 template <typename S, int N>
 ZG_HD void fwd_cast(const typename Traits<S>::Bits (&raw)[N], typename Traits<S>::Int (&v)[N],
                     int emax, bool special) {
   using T = Traits<S>;
-  using I = typename T::Int;
   const int se = T::kPrec - 2 - emax;
   const S s = pow2<S>(se);
   if (!special && se <= T::kEBias) {
 #pragma unroll (N <= 64 ? N : 1)
-    for (int i = 0; i < N; i++) v[i] = trunc_int<S>(fmul<S>(s, from_bits<S>(raw[i])));
-  } else {
-    const S lim = pow2<S>(T::kPrec - 1);
     for (int i = 0; i < N; i++) {
-      S x = fmul<S>(s, from_bits<S>(raw[i]));
-      v[i] = (x < lim && x > -lim) ? trunc_int<S>(x) : (I)((typename T::UInt)1 << (T::kPrec - 1));
+      if constexpr (sizeof(S) == 8) v[i] = scale_trunc<S>(raw[i], se);
+      else v[i] = trunc_int<S>(fmul<S>(s, from_bits<S>(raw[i])));
     }
+  } else {
+    for (int i = 0; i < N; i++) v[i] = cast_slow<S>(raw[i], s);
   }
 }
 
@@ -315,9 +384,46 @@ ZG_HD void fwd_cast(const typename Traits<S>::Bits (&raw)[N], typename Traits<S>
 template <typename S, int N>
 ZG_HD void inv_cast(const typename Traits<S>::Int (&v)[N], typename Traits<S>::Bits (&raw)[N], int emax) {
   using T = Traits<S>;
-  const S s = pow2<S>(emax - (T::kPrec - 2));
+  const int e = emax - (T::kPrec - 2);
+  if constexpr (sizeof(S) == 8) {
+    // every product normal: smallest |v| = 1 and largest 2^(P-1) stay in range
+    if (e >= 1 - T::kEBias && e + T::kPrec - 1 <= T::kEBias) {
+#pragma unroll (N <= 64 ? N : 1)
+      for (int i = 0; i < N; i++) raw[i] = int_scale<S>(v[i], e);
+      return;
+    }
+  }
+  const S s = pow2<S>(e);
 #pragma unroll (N <= 64 ? N : 1)
   for (int i = 0; i < N; i++) raw[i] = to_bits<S>(fmul<S>(s, int_to_float<S>(v[i])));
+}
+
+// Reversible floating-point blocks: does the block-floating-point cast
+// round-trip bit for bit (src/template/revencodef.c:9-16)?  When no value is
+// special and 2^(emax-(P-2)) is a normal number, both casts only scale by
+// powers of two, so the answer is yes exactly when no value is -0 and every
+// nonzero value's lowest set bit is worth at least 2^(emax-(P-2)).  Otherwise
+// each value is cast and cast back.  Nothing is kept, so the caller's raw
+// array is the only live copy of the block.
+template <typename S, int N>
+ZG_HD bool bfp_exact(const typename Traits<S>::Bits (&raw)[N], int emax, bool special) {
+  using T = Traits<S>;
+  using B = typename T::Bits;
+  const int lo = emax - (T::kPrec - 2);
+  bool exact = true;
+  if (!special && lo >= 1 - T::kEBias) {
+#pragma unroll (N <= 64 ? N : 1)
+    for (int i = 0; i < N; i++) {
+      int q;
+      const B m = significand<S>(raw[i], q);
+      exact &= m ? q + (int)ctz64((uint64_t)m) >= lo : raw[i] == 0;
+    }
+  } else {
+    const S s = pow2<S>(T::kPrec - 2 - emax), r = pow2<S>(lo);
+    for (int i = 0; i < N; i++)
+      exact &= to_bits<S>(fmul<S>(r, int_to_float<S>(cast_slow<S>(raw[i], s)))) == raw[i];
+  }
+  return exact;
 }
 
 // ---------------------------------------------------------------------------
@@ -753,17 +859,21 @@ ZG_HD unsigned decode_float_rev(Source& in, const BlockParams& p,
   if (in.read(1)) {
     I v[N];
     bits++;
-    if (in.read(1)) {
-      bits += rev_decode_ints<D>(in, p.minbits - umin(bits, p.minbits), p.maxbits - bits, v, pb);
+    const bool reinterpreted = in.read(1);   // one copy of the plane decoder for both kinds
+    int emax = 0;
+    if (!reinterpreted) {
+      bits += T::kEBits;
+      emax = (int)in.read(T::kEBits) - T::kEBias;
+    }
+    bits += rev_decode_ints<D>(in, p.minbits - umin(bits, p.minbits), p.maxbits - bits, v, pb);
+    if (reinterpreted) {
 #pragma unroll (N <= 64 ? N : 1)
       for (int i = 0; i < N; i++) raw[i] = v[i] < 0 ? ((B)v[i] ^ kTc) : (B)v[i];
+    } else if (emax != -T::kEBias) {
+      inv_cast<S, N>(v, raw, emax);
     } else {
-      bits += T::kEBits;
-      const int emax = (int)in.read(T::kEBits) - T::kEBias;
-      bits += rev_decode_ints<D>(in, p.minbits - umin(bits, p.minbits), p.maxbits - bits, v, pb);
-      if (emax != -T::kEBias) inv_cast<S, N>(v, raw, emax);
-      else
-        for (int i = 0; i < N; i++) raw[i] = 0;
+#pragma unroll (N <= 64 ? N : 1)
+      for (int i = 0; i < N; i++) raw[i] = 0;
     }
   } else {
 #pragma unroll (N <= 64 ? N : 1)
@@ -853,15 +963,13 @@ ZG_HD void prepare_coeffs(BlockHead& h, const BlockParams& p, const typename Tra
       return;
     }
     constexpr B kTc = ~(B(1) << (8 * sizeof(B) - 1));
-    bool exact = true;
+    bool exact;
     if (emax != -T::kEBias) {
-      fwd_cast<S, N>(raw, v, emax, special);
-      const S s = pow2<S>(emax - (T::kPrec - 2));
-#pragma unroll (N <= 64 ? N : 1)
-      for (int i = 0; i < N; i++) exact &= to_bits<S>(fmul<S>(s, int_to_float<S>(v[i]))) == raw[i];
+      exact = bfp_exact<S, N>(raw, emax, special);
     } else {
+      exact = true;
 #pragma unroll (N <= 64 ? N : 1)
-      for (int i = 0; i < N; i++) { v[i] = 0; exact &= raw[i] == 0; }
+      for (int i = 0; i < N; i++) exact &= raw[i] == 0;
     }
     unsigned outer;
     if (exact) {
@@ -870,6 +978,7 @@ ZG_HD void prepare_coeffs(BlockHead& h, const BlockParams& p, const typename Tra
         h.hdr = 0; h.hdr_bits = 1; h.coded = false; h.pad_to = 0;
         return;
       }
+      fwd_cast<S, N>(raw, v, emax, special);
       h.hdr = 1 | ((uint64_t)e << 2);
       outer = 2 + T::kEBits;
     } else {                                       // reinterpret sign-magnitude as two's complement
@@ -1020,6 +1129,79 @@ ZG_HD unsigned emit_block(Sink& out, const BlockHead& h, const uint64_t* plane, 
     out.pad(h.pad_to - bits);
     bits = h.pad_to;
   }
+  return bits;
+}
+
+// Position-addressed coder (N <= 64) for kernels that own a zeroed image.
+// Every plane's code starts at an offset known from the O(1) plane lengths,
+// so bits are OR-ed straight into place (out.set(pos, v, n): v clean, n <= 64,
+// pos relative to the block's first bit):
+//  pass 1, per plane: the n verbatim bits and, if anything above n is set,
+//    the opening positive group test; planes with such bits ("event planes")
+//    are remembered: the slot of plane k is overwritten with r = x >> n and
+//    base[k] receives the position of its opening test;
+//  pass 2, one flat loop over every one bit of every event plane: the j-th
+//    one at offset p of r sits at base + p + j + 1 and, unless it is the
+//    plane's last one, is followed by a positive test at base + p + j + 2;
+//    a last one at the last coefficient is implied and not written.
+// Zeros need no writes, and bits at or past the budget are dropped, which
+// cuts the code exactly where the reference's bit budget stops the coder
+// (src/template/encode.c:92-256).  The loops run per plane and per event of
+// the block, so the lanes of a warp diverge far less than with a loop per
+// event inside a loop per plane.  Returns the block's bits, as emit_block.
+template <int P, int N, class Out>
+ZG_HD unsigned emit_block_or(Out& out, const BlockHead& h, uint64_t* plane, int stride, uint16_t* base,
+                             int bstride) {
+  using Mask = typename std::conditional<(P <= 32), uint32_t, uint64_t>::type;
+  constexpr unsigned kImplied = 0x8000;   // base flag: the plane's last one is the implied last coefficient
+  if (h.hdr_bits) out.set(0, h.hdr, h.hdr_bits);
+  unsigned bits = h.hdr_bits;
+  if (h.coded) {
+    const int kmin = (unsigned)P > h.maxprec ? P - (int)h.maxprec : 0;
+    const uint64_t lim = (uint64_t)h.hdr_bits + h.budget;   // first dropped position
+    uint64_t at = h.hdr_bits;                               // start of the current plane's code
+    unsigned n = 0;
+    Mask events = 0;                                        // bit k: plane k has ones above its n
+    for (int k = P - 1; k >= kmin && at < lim; k--) {
+      const uint64_t x = plane[k * stride];
+      const unsigned n0 = n;
+      const unsigned len = plane_bits<N>(x, n);
+      if (n0) {
+        const unsigned m = (uint64_t)n0 < lim - at ? n0 : (unsigned)(lim - at);
+        out.set(at, low_bits(x, m), m);
+      }
+      if (n != n0 && at + n0 < lim) {                       // opening positive test of an event plane
+        out.set(at + n0, 1, 1);
+        plane[k * stride] = x >> n0;
+        base[k * bstride] = (uint16_t)((at + n0) | (n == (unsigned)N ? kImplied : 0u));
+        events |= Mask(1) << k;
+      }
+      at += len;
+    }
+    bits += (unsigned)((at < lim ? at : lim) - h.hdr_bits);
+    uint64_t r = 0;
+    unsigned b = 0, j = 0;
+    bool implied = false;
+    while (r || events) {
+      if (!r) {
+        const int k = 63 - clz64((uint64_t)events);
+        events &= ~(Mask(1) << k);
+        r = plane[k * stride];
+        const unsigned v = base[k * bstride];
+        b = v & (kImplied - 1);
+        implied = v & kImplied;
+        j = 0;
+      }
+      const uint64_t pos = (uint64_t)b + ctz64(r) + j + 1;
+      r &= r - 1;
+      j++;
+      if (pos < lim) {
+        if (r) out.set(pos, pos + 1 < lim ? 3 : 1, pos + 1 < lim ? 2 : 1);   // the one, then a positive test
+        else if (!implied) out.set(pos, 1, 1);                               // the plane's last one
+      }
+    }
+  }
+  if (bits < h.pad_to) bits = h.pad_to;
   return bits;
 }
 

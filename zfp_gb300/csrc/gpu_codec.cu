@@ -4,8 +4,10 @@
 // fixed-rate 1-3D contiguous fields; this path takes every mode, type,
 // dimensionality, stride layout and stream offset the serial codec takes
 // (src/zfp.c:1052-1180) and produces the same bits.  Per call:
-//   1. classify field and stream buffers (host or device); stage host data
-//      through device memory from the stream-ordered pool;
+//   1. classify field and stream buffers: device memory and page-locked
+//      host memory mapped into the device (read and written in place by the
+//      kernels, over the host link) are used as they are; other host data
+//      is staged through device memory from the stream-ordered pool;
 //   2. describe the field as one Job and launch the encode/decode kernel on
 //      the zfp_stream's CUDA stream;
 //   3. leave the bit stream as the serial path leaves it (flushed on
@@ -15,6 +17,7 @@
 // keyed by stream buffer and start bit, and the decoder verifies it.  For a
 // stream with no entry (written elsewhere) the offsets are recovered on the
 // GPU by a sequential parse.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -85,6 +88,43 @@ bool is_device_ptr(const void* p) {
   }
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
+
+// Page-locked host memory (cudaHostAlloc / cudaHostRegister) that the
+// device addresses at the same virtual address: kernels may read and write
+// it directly.  The whole range [p, p + bytes) must lie inside one such
+// allocation (the driver's allocation range), so no kernel touches a page
+// outside it; anything else is staged.
+bool is_mapped_host(const void* p, size_t bytes) {
+  if (!p || !bytes) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (a.type != cudaMemoryTypeHost || a.devicePointer != p || a.hostPointer != p) return false;
+  // the driver call is looked up at run time so the library loads without libcuda
+  using GetAttr = CUresult (*)(void*, CUpointer_attribute, CUdeviceptr);
+  static GetAttr get_attr = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      fn = nullptr;
+    }
+    return (GetAttr)fn;
+  }();
+  if (!get_attr) return false;
+  CUdeviceptr start = 0;
+  size_t size = 0;
+  if (get_attr(&start, CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, (CUdeviceptr)p) != CUDA_SUCCESS ||
+      get_attr(&size, CU_POINTER_ATTRIBUTE_RANGE_SIZE, (CUdeviceptr)p) != CUDA_SUCCESS)
+    return false;
+  const uintptr_t b = (uintptr_t)p;
+  return start && b >= (uintptr_t)start && bytes <= size && b - (uintptr_t)start <= size - bytes;
+}
+
+static thread_local size_t g_staged = 0;   // bytes copied host<->device by this thread's last call
 
 void init_pool_once() {
   static std::once_flag flag;
@@ -302,15 +342,24 @@ int persistent_grid() {
 }
 
 // decide shared- or global-memory staging and the grid
-static cudaError_t plan_launch(LaunchArgs& a, uint64_t bound_bits, uint32_t total_tiles, size_t extra_smem,
-                               DevBuf& gimg, cudaStream_t st) {
+// Launch geometry; a.one / a.jobs must be set (they select the kernel).
+// `bound_bits` bounds one block's code, so a tile's image never exceeds
+// `words`.  Encode: the image lives in shared memory up to the kernel's
+// occupancy room; when a tile may be larger, a persistent grid gets one
+// global slot per CTA for such tiles.  Decode: up to the room of a tile's
+// stream words is staged; larger tiles are read from the stream directly.
+static cudaError_t plan_launch(LaunchArgs& a, int type, int dims, bool encode, uint64_t bound_bits,
+                               uint32_t total_tiles, DevBuf& gimg, cudaStream_t st) {
   const uint64_t words = (uint64_t)kTile * bound_bits / 64 + 4;
+  const uint32_t room = stage_room_any(type, dims, a, encode);
   a.total_tiles = total_tiles;
-  a.img_words = (uint32_t)words;
-  a.gimg = nullptr;
   a.grid = (int)total_tiles;
-  if (words * 8 + extra_smem > kMaxTileSmem) {
+  a.gimg = nullptr;
+  a.slot_words = 0;
+  a.img_words = (uint32_t)std::min<uint64_t>(words, room);
+  if (encode && words > room) {
     a.grid = (int)std::min<uint64_t>(total_tiles, (uint64_t)persistent_grid());
+    a.slot_words = (uint32_t)words;
     cudaError_t e = gimg.alloc((size_t)a.grid * words * 8, st);
     if (e != cudaSuccess) return e;
     a.gimg = (uint64_t*)gimg.p;
@@ -344,6 +393,15 @@ cudaError_t launch_encode_any(int type, int dims, const LaunchArgs& a, cudaStrea
 
 cudaError_t launch_decode_any(int type, int dims, const LaunchArgs& a, cudaStream_t st) {
   return by_type(type, dims, [&](auto s, auto d) { return run_decode<decltype(s), decltype(d)::value>(a, st); });
+}
+
+uint32_t stage_room_any(int type, int dims, const LaunchArgs& a, bool encode) {
+  uint32_t r = 0;
+  by_type(type, dims, [&](auto s, auto d) {
+    r = stage_room<decltype(s), decltype(d)::value>(a, encode);
+    return cudaSuccess;
+  });
+  return r;
 }
 
 cudaError_t launch_parse_any(int type, int dims, const Job& j, cudaStream_t st) {
@@ -390,19 +448,23 @@ size_t gpu_compress(zfp_stream* z, const zfp_field* f) {
   const uint64_t max_end = bit0 + fi.nblocks * (fixed ? (uint64_t)z->maxbits : bound);
   if (fixed && (max_end + 63) / 64 > cap_words) return fail("zfp_compress: stream buffer too small");
 
+  const size_t span = (size_t)(fi.hi - fi.lo + 1) * fi.esize;
+  const char* fbegin = (const char*)f->data + fi.lo * (ptrdiff_t)fi.esize;
   const bool field_dev = is_device_ptr(f->data);
+  const bool field_map = !field_dev && is_mapped_host(fbegin, span);
   const bool stream_dev = is_device_ptr(ss.begin);
+  const bool stream_map = !stream_dev && is_mapped_host(ss.begin, cap_words * 8);
   cudaError_t e;
+  g_staged = 0;
 
   // field
   DevBuf fstage;
   void* dfield = f->data;
-  if (!field_dev) {
-    const size_t span = (size_t)(fi.hi - fi.lo + 1) * fi.esize;
+  if (!field_dev && !field_map) {
     if ((e = fstage.alloc(span, st)) != cudaSuccess) return fail_cuda("zfp_compress: staging alloc", e);
-    const char* src = (const char*)f->data + fi.lo * (ptrdiff_t)fi.esize;
-    if ((e = cudaMemcpyAsync(fstage.p, src, span, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+    if ((e = cudaMemcpyAsync(fstage.p, fbegin, span, cudaMemcpyHostToDevice, st)) != cudaSuccess)
       return fail_cuda("zfp_compress: field upload", e);
+    g_staged += span;
     dfield = (char*)fstage.p - fi.lo * (ptrdiff_t)fi.esize;
   }
 
@@ -411,7 +473,7 @@ size_t gpu_compress(zfp_stream* z, const zfp_field* f) {
   uint64_t* dwords = ss.begin;
   uint64_t dcap = cap_words;
   const uint64_t w_first = bit0 / 64;
-  if (!stream_dev) {
+  if (!stream_dev && !stream_map) {
     const uint64_t w_end = std::min<uint64_t>(cap_words, (max_end + 63) / 64);
     const uint64_t nw = w_end > w_first ? w_end - w_first : 0;
     if ((e = sstage.alloc(nw * 8, st)) != cudaSuccess) return fail_cuda("zfp_compress: staging alloc", e);
@@ -445,7 +507,7 @@ size_t gpu_compress(zfp_stream* z, const zfp_field* f) {
   a.sc = lm.sc;
   a.use_ticket = fixed ? 0 : 1;
   DevBuf gimg;
-  if ((e = plan_launch(a, fixed ? z->maxbits : bound, job.ntiles, plane_bytes(fi.esize, fi.dims), gimg, st)) !=
+  if ((e = plan_launch(a, fi.type, fi.dims, true, fixed ? z->maxbits : bound, job.ntiles, gimg, st)) !=
           cudaSuccess ||
       (e = launch_encode_any(fi.type, fi.dims, a, st)) != cudaSuccess)
     return fail_cuda("zfp_compress: launch", e);
@@ -466,12 +528,13 @@ size_t gpu_compress(zfp_stream* z, const zfp_field* f) {
                                              : "zfp_compress: GPU wait timed out");
   }
   const uint64_t end = res.end_bit;
-  if (!stream_dev) {
+  if (!stream_dev && !stream_map) {
     const uint64_t w_end = (end + 63) / 64;
     if ((e = cudaMemcpyAsync(ss.begin + w_first, dwords + w_first, (w_end - w_first) * 8, cudaMemcpyDeviceToHost,
                              st)) != cudaSuccess ||
         (e = cudaStreamSynchronize(st)) != cudaSuccess)
       return fail_cuda("zfp_compress: stream download", e);
+    g_staged += (w_end - w_first) * 8;
   }
   if (index) {
     registry_insert(make_entry(ss.begin, bit0, end, fi, job, index));   // written: the stream was synchronised
@@ -500,9 +563,14 @@ size_t gpu_decompress(zfp_stream* z, zfp_field* f) {
   const uint64_t cap_words = (uint64_t)(ss.end - ss.begin);
   const bool fixed = is_fixed_rate(fi, z);
   const uint64_t bound = block_bound(fi, z);
+  const size_t span = (size_t)(fi.hi - fi.lo + 1) * fi.esize;
+  char* fbegin = (char*)f->data + fi.lo * (ptrdiff_t)fi.esize;
   const bool field_dev = is_device_ptr(f->data);
+  const bool field_map = !field_dev && is_mapped_host(fbegin, span);
   const bool stream_dev = is_device_ptr(ss.begin);
+  const bool stream_map = !stream_dev && is_mapped_host(ss.begin, cap_words * 8);
   cudaError_t e;
+  g_staged = 0;
 
   uint64_t end = 0;
   IndexEntry ent;
@@ -520,12 +588,13 @@ size_t gpu_decompress(zfp_stream* z, zfp_field* f) {
   uint64_t* dwords = ss.begin;
   uint64_t dcap = cap_words;
   const uint64_t w_first = bit0 / 64;
-  if (!stream_dev) {
+  if (!stream_dev && !stream_map) {
     const uint64_t w_end = (fixed || have_index) ? std::min<uint64_t>(cap_words, (end + 63) / 64) : cap_words;
     const uint64_t nw = w_end > w_first ? w_end - w_first : 0;
     if ((e = sstage.alloc(nw * 8, st)) != cudaSuccess) return fail_cuda("zfp_decompress: staging alloc", e);
     if (nw && (e = cudaMemcpyAsync(sstage.p, ss.begin + w_first, nw * 8, cudaMemcpyHostToDevice, st)) != cudaSuccess)
       return fail_cuda("zfp_decompress: stream upload", e);
+    g_staged += nw * 8;
     dwords = (uint64_t*)sstage.p - w_first;
     dcap = w_first + nw;
   }
@@ -533,14 +602,13 @@ size_t gpu_decompress(zfp_stream* z, zfp_field* f) {
   // field
   DevBuf fstage;
   void* dfield = f->data;
-  const size_t span = (size_t)(fi.hi - fi.lo + 1) * fi.esize;
-  if (!field_dev) {
+  if (!field_dev && !field_map) {
     if ((e = fstage.alloc(span, st)) != cudaSuccess) return fail_cuda("zfp_decompress: staging alloc", e);
     const uint64_t count = (uint64_t)fi.n[0] * fi.n[1] * fi.n[2] * fi.n[3];
     if (count * fi.esize != span) {  // strided with gaps: keep what lies between the values
-      const char* src = (const char*)f->data + fi.lo * (ptrdiff_t)fi.esize;
-      if ((e = cudaMemcpyAsync(fstage.p, src, span, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+      if ((e = cudaMemcpyAsync(fstage.p, fbegin, span, cudaMemcpyHostToDevice, st)) != cudaSuccess)
         return fail_cuda("zfp_decompress: field upload", e);
+      g_staged += span;
     }
     dfield = (char*)fstage.p - fi.lo * (ptrdiff_t)fi.esize;
   }
@@ -586,8 +654,9 @@ size_t gpu_decompress(zfp_stream* z, zfp_field* f) {
   std::memset(&a, 0, sizeof a);
   a.njobs = 1;
   a.sc = lm.sc;
+  a.one = job;
   DevBuf gimg;
-  if ((e = plan_launch(a, fixed ? z->maxbits : bound, job.ntiles, plane_bytes(fi.esize, fi.dims), gimg, st)) !=
+  if ((e = plan_launch(a, fi.type, fi.dims, false, fixed ? z->maxbits : bound, job.ntiles, gimg, st)) !=
       cudaSuccess)
     return fail_cuda("zfp_decompress: plan", e);
   a.one = job;
@@ -609,11 +678,11 @@ size_t gpu_decompress(zfp_stream* z, zfp_field* f) {
         return fail_cuda("zfp_decompress: kernel", e);
     }
   }
-  if (!field_dev) {
-    char* dst = (char*)f->data + fi.lo * (ptrdiff_t)fi.esize;
-    if ((e = cudaMemcpyAsync(dst, fstage.p, span, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+  if (!field_dev && !field_map) {
+    if ((e = cudaMemcpyAsync(fbegin, fstage.p, span, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
         (e = cudaStreamSynchronize(st)) != cudaSuccess)
       return fail_cuda("zfp_decompress: field download", e);
+    g_staged += span;
   }
   if (parsed) registry_insert(make_entry(ss.begin, bit0, end, fi, job, parsed));
   set_stream_flushed(z->stream, end);
@@ -655,5 +724,7 @@ zfp_bool zfp_gb300_stream_synchronize(zfp_stream* z) {
 }
 
 const char* zfp_gb300_last_error(void) { return zg::g_last_error.c_str(); }
+
+size_t zfp_gb300_last_staged_bytes(void) { return zg::g_staged; }
 
 }  // extern "C"

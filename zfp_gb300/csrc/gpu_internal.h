@@ -92,6 +92,7 @@ bool registry_find(const void* begin, uint64_t bit0, const FieldInfo& fi, const 
 
 cudaError_t launch_encode_any(int type, int dims, const LaunchArgs& a, cudaStream_t st);
 cudaError_t launch_decode_any(int type, int dims, const LaunchArgs& a, cudaStream_t st);
+uint32_t stage_room_any(int type, int dims, const LaunchArgs& a, bool encode);
 cudaError_t launch_parse_any(int type, int dims, const Job& j, cudaStream_t st);
 
 }  // namespace zg

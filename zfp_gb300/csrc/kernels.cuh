@@ -224,6 +224,30 @@ struct SmemSink {
   }
 };
 
+// Position-addressed sink for emit_block_or: ORs bits into the tile image at
+// the block's start + pos.  Shared atomics, because the first and last words
+// of a block are shared with its neighbours; bits past the image are dropped
+// and flagged.
+struct ImgOr {
+  uint64_t* buf;
+  uint64_t start;     // block's first bit in the image
+  uint32_t cap;
+  unsigned* status;
+  // v must have no bits at or above n
+  __device__ __forceinline__ void set(uint64_t pos, uint64_t v, unsigned n) {
+    const uint64_t a = start + pos;
+    const uint32_t w = (uint32_t)(a >> 6);
+    const unsigned o = (unsigned)(a & 63);
+    const bool spill = o && o + n > 64;
+    if (w + (spill ? 1u : 0u) >= cap) {
+      atomicOr(status, (unsigned)kStatusOverflow);
+      return;
+    }
+    atomicOr((unsigned long long*)&buf[w], (unsigned long long)(v << o));
+    if (spill) atomicOr((unsigned long long*)&buf[w + 1], (unsigned long long)(v >> (64 - o)));
+  }
+};
+
 // ---------------------------------------------------------------------------
 // CTA-wide exclusive scan of one value per thread
 
@@ -347,9 +371,13 @@ __device__ __forceinline__ void write_tile(const Job& job, const LaunchScratch& 
 // ---------------------------------------------------------------------------
 // encode one tile
 
+// The tile image lives in shared memory (`simg`, `img_words` words) when the
+// tile's code fits there, else in this CTA's slot of global memory (`gslot`,
+// `slot_words` words, sized for the largest possible tile).
 template <typename S, int D, int kSel>
-__device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch& sc, uint32_t gt, uint64_t* img,
-                                            uint32_t img_words, uint64_t* planes) {
+__device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch& sc, uint32_t gt, uint64_t* simg,
+                                            uint32_t img_words, uint64_t* gslot, uint32_t slot_words,
+                                            uint64_t* planes) {
   using B = typename Traits<S>::Bits;
   using U = typename Traits<S>::UInt;
   constexpr int N = 1 << (2 * D);
@@ -382,7 +410,10 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
   uint32_t total;
   const uint32_t excl = cta_exclusive_scan(len, total, s_warp);
 
-  const uint32_t nw = min((total + 63) / 64 + 1, img_words);
+  const uint32_t need = (total + 63) / 64 + 1;
+  const bool in_smem = need <= img_words || !gslot;
+  uint64_t* img = in_smem ? simg : gslot;
+  const uint32_t nw = min(need, in_smem ? img_words : slot_words);
   for (uint32_t i = threadIdx.x; i < nw; i += kTile) img[i] = 0;
   if (fixed && threadIdx.x == 0) s_base = (unsigned long long)lt * kTile * job.maxbits;
   __syncthreads();
@@ -392,10 +423,14 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
     if (threadIdx.x == 0) s_base = before;
   }
   if (active) {
-    SmemSink out{img, excl >> 6, excl & 63u, 0ull, true, nw, &job.result->status};
-    if constexpr (N <= 64) emit_block<P, N>(out, h, my_planes, kTile);
-    else wc.emit(out);
-    out.finish();
+    if constexpr (N <= 64) {
+      ImgOr out{img, excl, nw, &job.result->status};
+      emit_block_or<P, N>(out, h, my_planes, kTile, (uint16_t*)(planes + P * kTile) + threadIdx.x, kTile);
+    } else {
+      SmemSink out{img, excl >> 6, excl & 63u, 0ull, true, nw, &job.result->status};
+      wc.emit(out);
+      out.finish();
+    }
   }
   __syncthreads();
 
@@ -405,10 +440,11 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
   if (threadIdx.x == 0 && lt + 1 == job.ntiles) job.result->end_bit = G + total;
 }
 
-// dynamic shared memory for the bit planes of one tile (1-3D blocks)
-template <typename S, int D>
+// dynamic shared memory for the bit planes of one tile (1-3D blocks); the
+// encoder also keeps a 16-bit code position per plane
+template <typename S, int D, bool kEncode>
 constexpr size_t plane_smem_bytes() {
-  return (1 << (2 * D)) <= 64 ? (size_t)8 * sizeof(typename Traits<S>::UInt) * kTile * 8 : 0;
+  return (1 << (2 * D)) <= 64 ? (size_t)8 * sizeof(typename Traits<S>::UInt) * kTile * (kEncode ? 10 : 8) : 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -496,10 +532,10 @@ __device__ __forceinline__ const Job* resolve_job(const Job& one, const Job* job
 template <typename S, int D, bool kMulti, int kSel>
 __global__ void __launch_bounds__(kTile) encode_kernel(const __grid_constant__ Job one, const Job* jobs, int njobs,
                                                        LaunchScratch sc, uint32_t total_tiles, int use_ticket,
-                                                       uint64_t* gimg, uint32_t img_words) {
+                                                       uint64_t* gimg, uint32_t slot_words, uint32_t img_words) {
   extern __shared__ uint64_t smem_img[];
-  uint64_t* img = gimg ? gimg + (size_t)blockIdx.x * img_words : smem_img;
-  uint64_t* planes = smem_img + (gimg ? 0 : img_words);
+  uint64_t* gslot = gimg ? gimg + (size_t)blockIdx.x * slot_words : nullptr;
+  uint64_t* planes = smem_img + img_words;
   __shared__ uint32_t s_tile;
   __shared__ Job s_job;
   for (uint32_t iter = blockIdx.x;; iter += gridDim.x) {
@@ -508,17 +544,19 @@ __global__ void __launch_bounds__(kTile) encode_kernel(const __grid_constant__ J
     const uint32_t gt = s_tile;
     if (gt >= total_tiles) break;
     const Job* job = resolve_job<kMulti>(one, jobs, njobs, gt, &s_job);
-    encode_tile<S, D, kSel>(*job, sc, gt, img, img_words, planes);
+    encode_tile<S, D, kSel>(*job, sc, gt, smem_img, img_words, gslot, slot_words, planes);
     __syncthreads();
   }
 }
 
+// img_words: shared memory for staging a tile's stream words; tiles that do
+// not fit are read from the stream directly
 template <typename S, int D, bool kMulti, int kSel>
 __global__ void __launch_bounds__(kTile) decode_kernel(const __grid_constant__ Job one, const Job* jobs, int njobs,
-                                                       uint32_t total_tiles, uint64_t* gimg, uint32_t img_words) {
+                                                       uint32_t total_tiles, uint32_t img_words) {
   extern __shared__ uint64_t smem_img[];
-  uint64_t* img = gimg ? gimg + (size_t)blockIdx.x * img_words : smem_img;
-  uint64_t* planes = smem_img + (gimg ? 0 : img_words);
+  uint64_t* img = smem_img;
+  uint64_t* planes = smem_img + img_words;
   __shared__ Job s_job;
   for (uint32_t gt = blockIdx.x; gt < total_tiles; gt += gridDim.x) {
     const Job* job = resolve_job<kMulti>(one, jobs, njobs, gt, &s_job);

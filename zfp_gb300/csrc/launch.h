@@ -15,8 +15,9 @@ struct LaunchArgs {
   LaunchScratch sc;
   uint32_t total_tiles;
   int use_ticket;
-  uint32_t img_words;     // staging words per tile
-  uint64_t* gimg;         // global staging (grid * img_words words) when shared memory is too small
+  uint32_t img_words;     // shared-memory words per CTA for the tile image / staged stream words
+  uint64_t* gimg;         // encode: one slot of slot_words per CTA for tiles larger than img_words
+  uint32_t slot_words;
   int grid;
 };
 
@@ -26,11 +27,19 @@ template <typename S, int D> cudaError_t run_encode(const LaunchArgs& a, cudaStr
 template <typename S, int D> cudaError_t run_decode(const LaunchArgs& a, cudaStream_t st);
 template <typename S, int D> cudaError_t run_parse(const Job& job, cudaStream_t st);
 
+// Shared-memory words a CTA of the kernel run_encode / run_decode would pick
+// for `a` can hold besides its bit planes without lowering the number of
+// CTAs its registers allow per SM.  Callers size img_words with it: up to
+// this many words the tile image (encode) or staged stream (decode) costs no
+// occupancy.
+template <typename S, int D> uint32_t stage_room(const LaunchArgs& a, bool encode);
+
 // a tile image plus bit planes larger than this is staged in global memory
 // instead (GB300 allows 227 KB of shared memory per CTA, static included)
 constexpr size_t kMaxTileSmem = 216 * 1024;
 
-// shared memory the encoder keeps for bit planes: 1-3D blocks only
-inline size_t plane_bytes(size_t esize, int dims) { return dims <= 3 ? esize * 8 * kTile * 8 : 0; }
+// shared memory the encoder keeps for bit planes and their code positions:
+// 1-3D blocks only (the decoder needs less)
+inline size_t plane_bytes(size_t esize, int dims) { return dims <= 3 ? esize * 8 * kTile * 10 : 0; }
 
 }  // namespace zg

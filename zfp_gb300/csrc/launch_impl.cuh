@@ -2,6 +2,7 @@
 // kern_{i32,i64,f32,f64}.cu.
 #pragma once
 
+#include <algorithm>
 #include <mutex>
 
 #include "kernels.cuh"
@@ -33,38 +34,76 @@ static void prepare_kernel() {
   std::call_once(flag, [] { allow_smem(Kernel); });
 }
 
+// Dynamic shared memory one CTA of Kernel may use while as many CTAs share
+// an SM as its registers allow (at most the opt-in limit).
+template <auto Kernel>
+static size_t smem_room() {
+  static const size_t room = [] {
+    int dev = 0, sm_smem = 0, reserved = 0;
+    cudaFuncAttributes fa;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa, Kernel) != cudaSuccess) {
+      cudaGetLastError();
+      return kMaxTileSmem;
+    }
+    const int regs = (fa.numRegs + 7) / 8 * 8;   // per-thread allocation granularity
+    const int ctas = regs > 0 ? std::max(1, 65536 / (regs * kTile)) : 1;
+    const size_t per = (size_t)sm_smem / ctas, fixed = (size_t)reserved + fa.sharedSizeBytes;
+    return std::min(per > fixed ? per - fixed : (size_t)0, kMaxTileSmem);
+  }();
+  return room;
+}
+
+template <auto K> struct KernelTag { static constexpr auto kernel = K; };
+
 // kernel variant: device job array -> multi-job kernel carrying both mode
 // paths; a single job -> the variant of its mode only
+template <typename S, int D, class F>
+static auto with_encoder(const LaunchArgs& a, F&& f) {
+  if (a.jobs) return f(KernelTag<encode_kernel<S, D, true, kAnyMode>>{});
+  if (a.one.minexp < kMinExp) return f(KernelTag<encode_kernel<S, D, false, kRevOnly>>{});
+  return f(KernelTag<encode_kernel<S, D, false, kLossyOnly>>{});
+}
+template <typename S, int D, class F>
+static auto with_decoder(const LaunchArgs& a, F&& f) {
+  if (a.jobs) return f(KernelTag<decode_kernel<S, D, true, kAnyMode>>{});
+  if (a.one.minexp < kMinExp) return f(KernelTag<decode_kernel<S, D, false, kRevOnly>>{});
+  return f(KernelTag<decode_kernel<S, D, false, kLossyOnly>>{});
+}
+
+template <typename S, int D>
+uint32_t stage_room(const LaunchArgs& a, bool encode) {
+  const size_t planes = encode ? plane_smem_bytes<S, D, true>() : plane_smem_bytes<S, D, false>();
+  auto words = [&](auto tag) -> uint32_t {
+    const size_t r = smem_room<decltype(tag)::kernel>();
+    return r > planes ? (uint32_t)((r - planes) / 8) : 0u;
+  };
+  return encode ? with_encoder<S, D>(a, words) : with_decoder<S, D>(a, words);
+}
+
 template <typename S, int D>
 cudaError_t run_encode(const LaunchArgs& a, cudaStream_t st) {
-  const size_t smem = (a.gimg ? 0 : (size_t)a.img_words * 8) + plane_smem_bytes<S, D>();
-  if (a.jobs) {
-    prepare_kernel<encode_kernel<S, D, true, kAnyMode>>();
-    encode_kernel<S, D, true, kAnyMode><<<a.grid, kTile, smem, st>>>(a.one, a.jobs, a.njobs, a.sc, a.total_tiles, a.use_ticket, a.gimg, a.img_words);
-  } else if (a.one.minexp < kMinExp) {
-    prepare_kernel<encode_kernel<S, D, false, kRevOnly>>();
-    encode_kernel<S, D, false, kRevOnly><<<a.grid, kTile, smem, st>>>(a.one, a.jobs, a.njobs, a.sc, a.total_tiles, a.use_ticket, a.gimg, a.img_words);
-  } else {
-    prepare_kernel<encode_kernel<S, D, false, kLossyOnly>>();
-    encode_kernel<S, D, false, kLossyOnly><<<a.grid, kTile, smem, st>>>(a.one, a.jobs, a.njobs, a.sc, a.total_tiles, a.use_ticket, a.gimg, a.img_words);
-  }
-  return cudaGetLastError();
+  const size_t smem = (size_t)a.img_words * 8 + plane_smem_bytes<S, D, true>();
+  return with_encoder<S, D>(a, [&](auto tag) {
+    constexpr auto kernel = decltype(tag)::kernel;
+    prepare_kernel<kernel>();
+    kernel<<<a.grid, kTile, smem, st>>>(a.one, a.jobs, a.njobs, a.sc, a.total_tiles, a.use_ticket, a.gimg,
+                                        a.slot_words, a.img_words);
+    return cudaGetLastError();
+  });
 }
 
 template <typename S, int D>
 cudaError_t run_decode(const LaunchArgs& a, cudaStream_t st) {
-  const size_t smem = (a.gimg ? 0 : (size_t)a.img_words * 8) + plane_smem_bytes<S, D>();
-  if (a.jobs) {
-    prepare_kernel<decode_kernel<S, D, true, kAnyMode>>();
-    decode_kernel<S, D, true, kAnyMode><<<a.grid, kTile, smem, st>>>(a.one, a.jobs, a.njobs, a.total_tiles, a.gimg, a.img_words);
-  } else if (a.one.minexp < kMinExp) {
-    prepare_kernel<decode_kernel<S, D, false, kRevOnly>>();
-    decode_kernel<S, D, false, kRevOnly><<<a.grid, kTile, smem, st>>>(a.one, a.jobs, a.njobs, a.total_tiles, a.gimg, a.img_words);
-  } else {
-    prepare_kernel<decode_kernel<S, D, false, kLossyOnly>>();
-    decode_kernel<S, D, false, kLossyOnly><<<a.grid, kTile, smem, st>>>(a.one, a.jobs, a.njobs, a.total_tiles, a.gimg, a.img_words);
-  }
-  return cudaGetLastError();
+  const size_t smem = (size_t)a.img_words * 8 + plane_smem_bytes<S, D, false>();
+  return with_decoder<S, D>(a, [&](auto tag) {
+    constexpr auto kernel = decltype(tag)::kernel;
+    prepare_kernel<kernel>();
+    kernel<<<a.grid, kTile, smem, st>>>(a.one, a.jobs, a.njobs, a.total_tiles, a.img_words);
+    return cudaGetLastError();
+  });
 }
 
 template <typename S, int D>
@@ -80,4 +119,5 @@ cudaError_t run_parse(const Job& job, cudaStream_t st) {
   template cudaError_t run_encode<S, D>(const LaunchArgs&, cudaStream_t);      \
   template cudaError_t run_decode<S, D>(const LaunchArgs&, cudaStream_t);      \
   template cudaError_t run_parse<S, D>(const Job&, cudaStream_t);              \
+  template uint32_t stage_room<S, D>(const LaunchArgs&, bool);                 \
   }

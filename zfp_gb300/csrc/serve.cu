@@ -168,10 +168,12 @@ static cudaError_t launch_batch(Server* s, Lane* lane) {
     a.sc.side_cnt = (unsigned int*)(p + 64 + t * 24);
     a.total_tiles = g.tiles;
     a.use_ticket = 1;
-    a.img_words = g.img_words;
+    // encode keeps whole tile images in shared memory (no global slots);
+    // decode stages only what fits the kernel's occupancy room
+    const bool enc = reqs[g.idx[0]]->direction == 0;
+    a.img_words = enc ? g.img_words : std::min(g.img_words, stage_room_any(g.type, g.dims, a, false));
     a.grid = (int)std::min<uint64_t>(g.tiles, (uint64_t)persistent_grid());
-    e = reqs[g.idx[0]]->direction == 0 ? launch_encode_any(g.type, g.dims, a, lane->st)
-                                       : launch_decode_any(g.type, g.dims, a, lane->st);
+    e = enc ? launch_encode_any(g.type, g.dims, a, lane->st) : launch_decode_any(g.type, g.dims, a, lane->st);
     if (e != cudaSuccess) return e;
   }
   if ((e = cudaMemcpyAsync(lane->host_results, base, reqs.size() * sizeof(JobResult), cudaMemcpyDeviceToHost,
