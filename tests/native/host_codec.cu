@@ -29,13 +29,14 @@ struct VecSink {
     pos += n;
   }
   ZG_HD void pad(unsigned n) { pos += n; }
+  ZG_HD void finish() {}
 };
 
-// Position-addressed sink for zg::emit_block_or: ORs v (n bits, clean) at
+// Positional sink for zg::emit_block_2p: ORs v (n bits, clean) at
 // bit start + pos.  Writes at or past `end` (the block's returned length,
 // checked after the block) are recorded as overruns.
 static bool g_or_overrun = false;
-static int g_coder = 0;   // 0: emit_block (sequential puts), 1: emit_block_or
+static int g_coder = 0;   // 0: emit_block (sequential puts), 1: emit_block_2p
 
 struct OrSink {
   uint64_t* words;
@@ -120,9 +121,9 @@ uint64_t compress_t(const Geom& g, const zg::BlockParams& p, const void* data, u
         zg::prepare_coeffs<S, D>(h, p, raw, u);
         if (h.coded) zg::store_planes<N>(u, plane, 1);
         OrSink os{words, out.pos};
-        const unsigned bits = zg::emit_block_or<P, N>(os, h, plane, 1, base, 1);
-        if (os.hi > bits) g_or_overrun = true;
-        out.pos += bits;
+        const uint64_t at = out.pos;
+        const unsigned bits = zg::emit_block_2p<P, N>(out, os, h, plane, 1, base, 1);
+        if (os.hi > bits || out.pos != at + bits) g_or_overrun = true;
         continue;
       }
     }

@@ -68,8 +68,8 @@ SPECIAL = {np.float32: np.array([0.0, -0.0, 1e-45, -1e-45, 1e-40, 3.4e38, -3.4e3
 @pytest.mark.parametrize("dtype", [np.float32, np.float64, np.int32, np.int64], ids=lambda d: np.dtype(d).name)
 def test_device_codec_on_host_matches_oracle(host, oracle, dims, dtype, coder):
     """Both plane coders of codec.cuh: emit_block (sequential puts) and
-    emit_block_or (bits OR-ed at computed positions, used by the encoder
-    kernel for 1-3D blocks)."""
+    emit_block_2p (a sequential pass plus a pass that ORs event bits at
+    computed positions, used by the encoder kernel for 1-3D blocks)."""
     host.zgh_set_coder(1 if coder == "positional" else 0)
     rng = np.random.default_rng(dims * 10 + ZTYPE[np.dtype(dtype)])
     modes = [("rate", 4), ("rate", 12.5), ("rate", 1), ("precision", 7), ("precision", 20), ("accuracy", 1e-3),

@@ -221,7 +221,7 @@ zfp_gb300_batch* zfp_gb300_batch_create(zfp_stream* const* streams, const zfp_fi
     b->jobs[i].tile0 = g.total_tiles;
     g.total_tiles += b->jobs[i].ntiles;
     const uint64_t bound = fixed ? (uint64_t)z->maxbits : block_bound(fi, z);
-    g.tile_words = std::max<uint32_t>(g.tile_words, (uint32_t)((uint64_t)kTile * bound / 64 + 4));
+    g.tile_words = std::max<uint32_t>(g.tile_words, (uint32_t)image_words((uint64_t)kTile * bound / 64 + 4));
     g.members.push_back(i);
   }
   if (offset_words) {

@@ -1132,76 +1132,85 @@ ZG_HD unsigned emit_block(Sink& out, const BlockHead& h, const uint64_t* plane, 
   return bits;
 }
 
-// Position-addressed coder (N <= 64) for kernels that own a zeroed image.
-// Every plane's code starts at an offset known from the O(1) plane lengths,
-// so bits are OR-ed straight into place (out.set(pos, v, n): v clean, n <= 64,
-// pos relative to the block's first bit):
-//  pass 1, per plane: the n verbatim bits and, if anything above n is set,
-//    the opening positive group test; planes with such bits ("event planes")
-//    are remembered: the slot of plane k is overwritten with r = x >> n and
-//    base[k] receives the position of its opening test;
-//  pass 2, one flat loop over every one bit of every event plane: the j-th
-//    one at offset p of r sits at base + p + j + 1 and, unless it is the
-//    plane's last one, is followed by a positive test at base + p + j + 2;
-//    a last one at the last coefficient is implied and not written.
+// Two-pass coder (N <= 64) for kernels that own a zeroed image.  Every
+// plane's code starts at an offset known from the O(1) plane lengths:
+//  pass 1, through the sequential sink `seq`: per plane the n verbatim bits
+//    and, if anything above n is set, the opening positive group test; the
+//    rest of the plane's code is skipped (pad) and filled in by pass 2.
+//    Planes with such bits ("event planes") are remembered: the slot of
+//    plane k is overwritten with r = x >> n and base[k] receives the
+//    position of its opening test;
+//  pass 2, one flat loop over every one bit of every event plane, through
+//    the positional sink `pos` (out.set(at, v, n): OR v, n bits, at the
+//    block-relative bit `at`): the j-th one at offset p of r sits at
+//    base + p + j + 1 and, unless it is the plane's last one, is followed by
+//    a positive test at base + p + j + 2; a last one at the last coefficient
+//    is implied and not written.
 // Zeros need no writes, and bits at or past the budget are dropped, which
 // cuts the code exactly where the reference's bit budget stops the coder
-// (src/template/encode.c:92-256).  The loops run per plane and per event of
-// the block, so the lanes of a warp diverge far less than with a loop per
-// event inside a loop per plane.  Returns the block's bits, as emit_block.
-template <int P, int N, class Out>
-ZG_HD unsigned emit_block_or(Out& out, const BlockHead& h, uint64_t* plane, int stride, uint16_t* base,
+// (src/template/encode.c:92-256).  Pass 2 runs once per event of the block
+// rather than once per event inside a loop per plane, so the lanes of a warp
+// diverge far less.  Returns the block's bits, as emit_block.
+template <int P, int N, class Seq, class Pos>
+ZG_HD unsigned emit_block_2p(Seq& seq, Pos& pos, const BlockHead& h, uint64_t* plane, int stride, uint16_t* base,
                              int bstride) {
   using Mask = typename std::conditional<(P <= 32), uint32_t, uint64_t>::type;
   constexpr unsigned kImplied = 0x8000;   // base flag: the plane's last one is the implied last coefficient
-  if (h.hdr_bits) out.set(0, h.hdr, h.hdr_bits);
+  seq.put(h.hdr, h.hdr_bits);
   unsigned bits = h.hdr_bits;
+  Mask events = 0;                        // bit k: plane k has ones above its n
+  uint64_t lim = 0;
   if (h.coded) {
     const int kmin = (unsigned)P > h.maxprec ? P - (int)h.maxprec : 0;
-    const uint64_t lim = (uint64_t)h.hdr_bits + h.budget;   // first dropped position
+    lim = (uint64_t)h.hdr_bits + h.budget;                  // first dropped position
     uint64_t at = h.hdr_bits;                               // start of the current plane's code
     unsigned n = 0;
-    Mask events = 0;                                        // bit k: plane k has ones above its n
     for (int k = P - 1; k >= kmin && at < lim; k--) {
       const uint64_t x = plane[k * stride];
       const unsigned n0 = n;
       const unsigned len = plane_bits<N>(x, n);
-      if (n0) {
-        const unsigned m = (uint64_t)n0 < lim - at ? n0 : (unsigned)(lim - at);
-        out.set(at, low_bits(x, m), m);
-      }
-      if (n != n0 && at + n0 < lim) {                       // opening positive test of an event plane
-        out.set(at + n0, 1, 1);
+      const unsigned room = (uint64_t)len < lim - at ? len : (unsigned)(lim - at);
+      const unsigned m = n0 < room ? n0 : room;
+      seq.put(low_bits(x, m), m);
+      unsigned rest = room - m;
+      if (rest && n != n0) {                                // opening positive test of an event plane
+        seq.put(1, 1);
+        rest--;
         plane[k * stride] = x >> n0;
         base[k * bstride] = (uint16_t)((at + n0) | (n == (unsigned)N ? kImplied : 0u));
         events |= Mask(1) << k;
       }
+      seq.pad(rest);
       at += len;
     }
     bits += (unsigned)((at < lim ? at : lim) - h.hdr_bits);
-    uint64_t r = 0;
-    unsigned b = 0, j = 0;
-    bool implied = false;
-    while (r || events) {
-      if (!r) {
-        const int k = 63 - clz64((uint64_t)events);
-        events &= ~(Mask(1) << k);
-        r = plane[k * stride];
-        const unsigned v = base[k * bstride];
-        b = v & (kImplied - 1);
-        implied = v & kImplied;
-        j = 0;
-      }
-      const uint64_t pos = (uint64_t)b + ctz64(r) + j + 1;
-      r &= r - 1;
-      j++;
-      if (pos < lim) {
-        if (r) out.set(pos, pos + 1 < lim ? 3 : 1, pos + 1 < lim ? 2 : 1);   // the one, then a positive test
-        else if (!implied) out.set(pos, 1, 1);                               // the plane's last one
-      }
+  }
+  if (bits < h.pad_to) {
+    seq.pad(h.pad_to - bits);
+    bits = h.pad_to;
+  }
+  seq.finish();
+  uint64_t r = 0;
+  unsigned b = 0, j = 0;
+  bool implied = false;
+  while (r || events) {
+    if (!r) {
+      const int k = 63 - clz64((uint64_t)events);
+      events &= ~(Mask(1) << k);
+      r = plane[k * stride];
+      const unsigned v = base[k * bstride];
+      b = v & (kImplied - 1);
+      implied = v & kImplied;
+      j = 0;
+    }
+    const uint64_t at = (uint64_t)b + ctz64(r) + j + 1;
+    r &= r - 1;
+    j++;
+    if (at < lim) {
+      if (r) pos.set(at, at + 1 < lim ? 3 : 1, at + 1 < lim ? 2 : 1);   // the one, then a positive test
+      else if (!implied) pos.set(at, 1, 1);                             // the plane's last one
     }
   }
-  if (bits < h.pad_to) bits = h.pad_to;
   return bits;
 }
 
@@ -1294,8 +1303,9 @@ struct WordSourceT {
 
   ZG_HD uint64_t load(uint64_t i) const {
 #if defined(__CUDA_ARCH__)
+    // shared staging keeps a spare word after every 16 (bank spreading)
     if constexpr (kGlobal) return i < cap ? __ldg((const unsigned long long*)base + i) : 0ull;
-    else return i < cap ? base[i] : 0ull;
+    else return i < cap ? base[i + (i >> 4)] : 0ull;
 #else
     return i < cap ? base[i] : 0ull;
 #endif

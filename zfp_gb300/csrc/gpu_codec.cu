@@ -350,7 +350,7 @@ int persistent_grid() {
 // stream words is staged; larger tiles are read from the stream directly.
 static cudaError_t plan_launch(LaunchArgs& a, int type, int dims, bool encode, uint64_t bound_bits,
                                uint32_t total_tiles, DevBuf& gimg, cudaStream_t st) {
-  const uint64_t words = (uint64_t)kTile * bound_bits / 64 + 4;
+  const uint64_t words = image_words((uint64_t)kTile * bound_bits / 64 + 4);
   const uint32_t room = stage_room_any(type, dims, a, encode);
   a.total_tiles = total_tiles;
   a.grid = (int)total_tiles;

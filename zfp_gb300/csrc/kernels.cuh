@@ -171,6 +171,15 @@ __device__ __forceinline__ void scatter(const Job& job, uint64_t b, const B (&ra
 // are combined with atomicOr, every word in between belongs to it alone.
 // The image is zeroed beforehand, so padding only moves the cursor.
 
+// Tile images and staged stream words are stored with one spare 64-bit word
+// after every 16: a block of 512 bits (rate 8 in 3D) would otherwise put the
+// same word of every thread's block in the same shared-memory bank.  The
+// logical word w lives at img_phys(w); a buffer of `phys` words holds
+// img_cap(phys) logical words.
+__host__ __device__ constexpr uint32_t img_phys(uint32_t w) { return w + (w >> 4); }
+__host__ __device__ constexpr uint32_t img_cap(uint32_t phys) { return (uint32_t)((uint64_t)phys * 16 / 17); }
+
+
 struct SmemSink {
   uint64_t* buf;
   uint32_t word;
@@ -187,10 +196,10 @@ struct SmemSink {
       return;
     }
     if (first) {
-      atomicOr((unsigned long long*)&buf[word], (unsigned long long)w);
+      atomicOr((unsigned long long*)&buf[img_phys(word)], (unsigned long long)w);
       first = false;
     } else {
-      buf[word] = w;
+      buf[img_phys(word)] = w;
     }
     word++;
   }
@@ -219,32 +228,37 @@ struct SmemSink {
   }
   __device__ __forceinline__ void finish() {
     if (!fill) return;
-    if (word < cap) atomicOr((unsigned long long*)&buf[word], (unsigned long long)acc);
+    if (word < cap) atomicOr((unsigned long long*)&buf[img_phys(word)], (unsigned long long)acc);
     else atomicOr(status, (unsigned)kStatusOverflow);
   }
 };
 
-// Position-addressed sink for emit_block_or: ORs bits into the tile image at
-// the block's start + pos.  Shared atomics, because the first and last words
-// of a block are shared with its neighbours; bits past the image are dropped
-// and flagged.
+// Positional sink of emit_block_2p: ORs bits into the tile image at the
+// block's start + pos with 32-bit shared atomics (a block's first and last
+// words may hold a neighbour's bits).  `cap` counts logical 64-bit words;
+// bits past it are dropped and flagged.
 struct ImgOr {
   uint64_t* buf;
   uint64_t start;     // block's first bit in the image
   uint32_t cap;
   unsigned* status;
-  // v must have no bits at or above n
+  __device__ __forceinline__ void or32(uint32_t w, unsigned v) {
+    atomicOr((unsigned*)buf + 2 * img_phys(w >> 1) + (w & 1), v);
+  }
+  // v must have no bits at or above n (n <= 64)
   __device__ __forceinline__ void set(uint64_t pos, uint64_t v, unsigned n) {
     const uint64_t a = start + pos;
-    const uint32_t w = (uint32_t)(a >> 6);
-    const unsigned o = (unsigned)(a & 63);
-    const bool spill = o && o + n > 64;
-    if (w + (spill ? 1u : 0u) >= cap) {
+    const uint32_t w = (uint32_t)(a >> 5);
+    const unsigned o = (unsigned)(a & 31);
+    const unsigned end = o + n;                  // bits spanned from the first 32-bit word
+    if ((uint64_t)w + (end + 31) / 32 > 2ull * cap) {   // 32-bit words past the image
       atomicOr(status, (unsigned)kStatusOverflow);
       return;
     }
-    atomicOr((unsigned long long*)&buf[w], (unsigned long long)(v << o));
-    if (spill) atomicOr((unsigned long long*)&buf[w + 1], (unsigned long long)(v >> (64 - o)));
+    const uint64_t lo = v << o;
+    or32(w, (unsigned)lo);
+    if (end > 32) or32(w + 1, (unsigned)(lo >> 32));
+    if (end > 64) or32(w + 2, (unsigned)(v >> (64 - o)));
   }
 };
 
@@ -358,8 +372,8 @@ __device__ __forceinline__ void write_tile(const Job& job, const LaunchScratch& 
   const uint64_t wend = te ? tw + 1 : tw;
   for (uint64_t w = hw + threadIdx.x; w < wend; w += kTile) {
     const uint64_t j = w - hw;
-    const uint64_t cur = j < nimg ? img[j] : 0ull;
-    const uint64_t prev = j && j - 1 < nimg ? img[j - 1] : 0ull;
+    const uint64_t cur = j < nimg ? img[img_phys((uint32_t)j)] : 0ull;
+    const uint64_t prev = j && j - 1 < nimg ? img[img_phys((uint32_t)j - 1)] : 0ull;
     uint64_t v = sh ? (cur << sh) | (prev >> (64 - sh)) : cur;
     if (w == hw && first && sh) v |= job.head_word & ((1ull << sh) - 1);
     if (w == hw && sh && !first) merge_word(job, sc, gt, 1, w, v);
@@ -411,10 +425,10 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
   const uint32_t excl = cta_exclusive_scan(len, total, s_warp);
 
   const uint32_t need = (total + 63) / 64 + 1;
-  const bool in_smem = need <= img_words || !gslot;
+  const bool in_smem = need <= img_cap(img_words) || !gslot;
   uint64_t* img = in_smem ? simg : gslot;
-  const uint32_t nw = min(need, in_smem ? img_words : slot_words);
-  for (uint32_t i = threadIdx.x; i < nw; i += kTile) img[i] = 0;
+  const uint32_t nw = min(need, img_cap(in_smem ? img_words : slot_words));
+  for (uint32_t i = threadIdx.x; i < nw; i += kTile) img[img_phys(i)] = 0;
   if (fixed && threadIdx.x == 0) s_base = (unsigned long long)lt * kTile * job.maxbits;
   __syncthreads();
 
@@ -424,8 +438,9 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
   }
   if (active) {
     if constexpr (N <= 64) {
-      ImgOr out{img, excl, nw, &job.result->status};
-      emit_block_or<P, N>(out, h, my_planes, kTile, (uint16_t*)(planes + P * kTile) + threadIdx.x, kTile);
+      SmemSink seq{img, excl >> 6, excl & 63u, 0ull, true, nw, &job.result->status};
+      ImgOr pos{img, excl, nw, &job.result->status};
+      emit_block_2p<P, N>(seq, pos, h, my_planes, kTile, (uint16_t*)(planes + P * kTile) + threadIdx.x, kTile);
     } else {
       SmemSink out{img, excl >> 6, excl & 63u, 0ull, true, nw, &job.result->status};
       wc.emit(out);
@@ -477,10 +492,10 @@ __device__ __forceinline__ void decode_tile(const Job& job, uint32_t gt, uint64_
   }
   const uint64_t w0 = Gs >> 6;
   const uint64_t nwords = Ge >= Gs ? ((Ge + 63) >> 6) - w0 + 2 : ~0ull;
-  const bool staged = nwords <= img_words;
+  const bool staged = nwords <= img_cap(img_words);
   if (staged) {
     for (uint64_t i = threadIdx.x; i < nwords; i += kTile)
-      img[i] = w0 + i < job.cap_words ? __ldg((const unsigned long long*)job.words + w0 + i) : 0ull;
+      img[img_phys((uint32_t)i)] = w0 + i < job.cap_words ? __ldg((const unsigned long long*)job.words + w0 + i) : 0ull;
   }
   __syncthreads();
   if (!active) return;

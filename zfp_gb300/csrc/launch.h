@@ -34,6 +34,10 @@ template <typename S, int D> cudaError_t run_parse(const Job& job, cudaStream_t 
 // occupancy.
 template <typename S, int D> uint32_t stage_room(const LaunchArgs& a, bool encode);
 
+// 64-bit words of storage for `logical` words of tile image or staged stream:
+// the kernels keep a spare word after every 16 (shared-memory bank spreading)
+inline uint64_t image_words(uint64_t logical) { return logical + logical / 16 + 1; }
+
 // a tile image plus bit planes larger than this is staged in global memory
 // instead (GB300 allows 227 KB of shared memory per CTA, static included)
 constexpr size_t kMaxTileSmem = 216 * 1024;

@@ -73,7 +73,7 @@ extern "C" size_t zfp_gb300_compress_noalloc(zfp_stream* z, const zfp_field* f) 
     return fail("zfp_gb300_compress_noalloc: field has more than 4194304 blocks (the scratch limit)");
   const bool fixed = is_fixed_rate(fi, z);
   const uint64_t bound = fixed ? (uint64_t)z->maxbits : block_bound(fi, z);
-  const uint64_t img_words = (uint64_t)kTile * bound / 64 + 4;
+  const uint64_t img_words = image_words((uint64_t)kTile * bound / 64 + 4);
   if (img_words * 8 + plane_bytes(fi.esize, fi.dims) > kMaxTileSmem)
     return fail("zfp_gb300_compress_noalloc: blocks too large for shared-memory staging");
   const uint64_t bit0 = (uint64_t)(ss.ptr - ss.begin) * 64 + ss.bits;

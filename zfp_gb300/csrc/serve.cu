@@ -109,7 +109,7 @@ static cudaError_t launch_batch(Server* s, Lane* lane) {
       r.job.tile0 = g.tiles;
       g.tiles += r.job.ntiles;
       const uint64_t bound = r.fixed ? (uint64_t)r.z->maxbits : block_bound(r.fi, r.z);
-      g.img_words = std::max<uint32_t>(g.img_words, (uint32_t)((uint64_t)kTile * bound / 64 + 4));
+      g.img_words = std::max<uint32_t>(g.img_words, (uint32_t)image_words((uint64_t)kTile * bound / 64 + 4));
     }
     g.jobs_off = off;
     off += ((g.idx.size() * sizeof(Job)) + 255) & ~(size_t)255;
@@ -332,7 +332,7 @@ uint64_t zfp_gb300_server_submit(zfp_gb300_server* s, zfp_stream* z, const zfp_f
   const FieldInfo& fi = r->fi;
   r->fixed = is_fixed_rate(fi, z);
   const uint64_t bound = r->fixed ? (uint64_t)z->maxbits : block_bound(fi, z);
-  if (((uint64_t)kTile * bound / 64 + 4) * 8 + plane_bytes(fi.esize, fi.dims) > kMaxTileSmem) {
+  if (image_words((uint64_t)kTile * bound / 64 + 4) * 8 + plane_bytes(fi.esize, fi.dims) > kMaxTileSmem) {
     fail("zfp_gb300_server_submit: blocks too large for shared-memory staging");
     return 0;
   }
