@@ -665,8 +665,11 @@ struct PlaneBuf {
   int stride;
 };
 
+// Planes below the last one decoded are zero.  For 64-bit coefficients,
+// when every decoded plane lies in the top half, only the top half is
+// stored (zeros included) and `top_only` is set: the low words are zero.
 template <int P, int N, class Source>
-ZG_HD unsigned decode_planes(Source& in, unsigned budget, unsigned maxprec, PlaneBuf pb) {
+ZG_HD unsigned decode_planes(Source& in, unsigned budget, unsigned maxprec, PlaneBuf pb, bool& top_only) {
   const int kmin = (unsigned)P > maxprec ? P - (int)maxprec : 0;
   unsigned bits = budget, n = 0;
   int k = P - 1;
@@ -701,7 +704,8 @@ ZG_HD unsigned decode_planes(Source& in, unsigned budget, unsigned maxprec, Plan
     }
     pb.p[k * pb.stride] = x;
   }
-  for (; k >= 0; k--) pb.p[k * pb.stride] = 0;
+  top_only = P == 64 && N > 4 && k >= 31;
+  for (const int kz = top_only ? 32 : 0; k >= kz; k--) pb.p[k * pb.stride] = 0;
   return budget - bits;
 }
 
@@ -781,7 +785,20 @@ ZG_HD unsigned uncode_coeffs(Source& in, unsigned budget, unsigned maxprec,
   constexpr int N = 1 << (2 * D);
   constexpr int P = 8 * sizeof(U);
   if constexpr (N <= 64) {
-    const unsigned bits = decode_planes<P, N>(in, budget, maxprec, pb);
+    bool top_only;
+    const unsigned bits = decode_planes<P, N>(in, budget, maxprec, pb, top_only);
+    if constexpr (P == 64 && N > 4) {
+      if (top_only) {
+        uint64_t pl[32];
+#pragma unroll
+        for (int k = 0; k < 32; k++) pl[k] = pb.p[(32 + k) * pb.stride];
+        uint32_t hi[N];
+        take_planes<N>(pl, hi);
+#pragma unroll
+        for (int i = 0; i < N; i++) u[i] = (U)hi[i] << 32;
+        return bits;
+      }
+    }
     uint64_t pl[P];
 #pragma unroll
     for (int k = 0; k < P; k++) pl[k] = pb.p[k * pb.stride];
@@ -1033,12 +1050,13 @@ ZG_HD unsigned plane_bits(uint64_t x, unsigned& n) {
     if (!r) {
       len += 1;
     } else {
-      const unsigned hb = 63 - (unsigned)clz64(r);
-      const unsigned ones = (unsigned)popc64(r);
-      len += hb + 1 + ones;
-      if (n + hb + 1 < (unsigned)N) len += 1;   // closing negative group test
-      else len -= 1;                            // last coefficient's one is implied
-      n += hb + 1;
+      // the top one of x is the top one of r: n verbatim bits, then a test
+      // and a bit per coefficient up to it, a test after each one, and a
+      // closing negative test (none when the last coefficient is reached,
+      // whose one is then implied)
+      const unsigned top = 64 - (unsigned)clz64(x);
+      len = top + (unsigned)popc64(r) + (top < (unsigned)N ? 1u : 0u) - (top < (unsigned)N ? 0u : 1u);
+      n = top;
     }
   }
   return len;
@@ -1159,31 +1177,31 @@ ZG_HD unsigned emit_block_2p(Seq& seq, Pos& pos, const BlockHead& h, uint64_t* p
   seq.put(h.hdr, h.hdr_bits);
   unsigned bits = h.hdr_bits;
   Mask events = 0;                        // bit k: plane k has ones above its n
-  uint64_t lim = 0;
+  // positions fit 16 bits: a block's code is at most P * (N + 2) + N bits
+  unsigned lim = 0;
   if (h.coded) {
     const int kmin = (unsigned)P > h.maxprec ? P - (int)h.maxprec : 0;
-    lim = (uint64_t)h.hdr_bits + h.budget;                  // first dropped position
-    uint64_t at = h.hdr_bits;                               // start of the current plane's code
+    const uint64_t lim64 = (uint64_t)h.hdr_bits + h.budget;  // first dropped position
+    lim = lim64 < 0x7fffu ? (unsigned)lim64 : 0x7fffu;
+    unsigned at = h.hdr_bits;                                // start of the current plane's code
     unsigned n = 0;
     for (int k = P - 1; k >= kmin && at < lim; k--) {
       const uint64_t x = plane[k * stride];
       const unsigned n0 = n;
       const unsigned len = plane_bits<N>(x, n);
-      const unsigned room = (uint64_t)len < lim - at ? len : (unsigned)(lim - at);
+      const unsigned room = len < lim - at ? len : lim - at;
       const unsigned m = n0 < room ? n0 : room;
-      seq.put(low_bits(x, m), m);
-      unsigned rest = room - m;
-      if (rest && n != n0) {                                // opening positive test of an event plane
-        seq.put(1, 1);
-        rest--;
+      const unsigned ev = n != n0 && room > m;               // opening positive test of an event plane
+      seq.put(low_bits(x, m) | ((uint64_t)ev << m), m + ev);
+      if (ev) {
         plane[k * stride] = x >> n0;
         base[k * bstride] = (uint16_t)((at + n0) | (n == (unsigned)N ? kImplied : 0u));
         events |= Mask(1) << k;
       }
-      seq.pad(rest);
+      seq.pad(room - m - ev);
       at += len;
     }
-    bits += (unsigned)((at < lim ? at : lim) - h.hdr_bits);
+    bits += (at < lim ? at : lim) - h.hdr_bits;
   }
   if (bits < h.pad_to) {
     seq.pad(h.pad_to - bits);
@@ -1191,7 +1209,7 @@ ZG_HD unsigned emit_block_2p(Seq& seq, Pos& pos, const BlockHead& h, uint64_t* p
   }
   seq.finish();
   uint64_t r = 0;
-  unsigned b = 0, j = 0;
+  unsigned b = 0;
   bool implied = false;
   while (r || events) {
     if (!r) {
@@ -1199,13 +1217,12 @@ ZG_HD unsigned emit_block_2p(Seq& seq, Pos& pos, const BlockHead& h, uint64_t* p
       events &= ~(Mask(1) << k);
       r = plane[k * stride];
       const unsigned v = base[k * bstride];
-      b = v & (kImplied - 1);
+      b = (v & (kImplied - 1)) + 1;     // the j-th one at offset p sits at b + p + j
       implied = v & kImplied;
-      j = 0;
     }
-    const uint64_t at = (uint64_t)b + ctz64(r) + j + 1;
+    const unsigned at = b + ctz64(r);
     r &= r - 1;
-    j++;
+    b++;
     if (at < lim) {
       if (r) pos.set(at, at + 1 < lim ? 3 : 1, at + 1 < lim ? 2 : 1);   // the one, then a positive test
       else if (!implied) pos.set(at, 1, 1);                             // the plane's last one
@@ -1214,10 +1231,24 @@ ZG_HD unsigned emit_block_2p(Seq& seq, Pos& pos, const BlockHead& h, uint64_t* p
   return bits;
 }
 
-// coefficients -> planes stored at plane[k * stride]
+// coefficients -> planes stored at plane[k * stride].  64-bit coefficients
+// whose coded planes all lie in the top half (maxprec <= 32: every lossy
+// mode but high precision) transpose only their high words.
 template <int N, typename U>
-ZG_HD void store_planes(const U (&u)[N], uint64_t* plane, int stride) {
+ZG_HD void store_planes(const U (&u)[N], uint64_t* plane, int stride, unsigned maxprec = 8 * sizeof(U)) {
   constexpr int P = 8 * sizeof(U);
+  if constexpr (P == 64 && N > 4) {
+    if (maxprec <= 32) {
+      uint32_t hi[N];
+#pragma unroll
+      for (int i = 0; i < N; i++) hi[i] = (uint32_t)(u[i] >> 32);
+      uint64_t pl[32];
+      make_planes<N>(hi, pl);
+#pragma unroll
+      for (int k = 0; k < 32; k++) plane[(32 + k) * stride] = pl[k];
+      return;
+    }
+  }
   uint64_t pl[P];
   make_planes<N>(u, pl);
 #pragma unroll
@@ -1253,7 +1284,7 @@ ZG_HD unsigned encode_block(Sink& out, const BlockParams& p, const typename Trai
     U u[N];
     uint64_t plane[8 * sizeof(U)];
     prepare_coeffs<S, D>(h, p, raw, u);
-    if (h.coded) store_planes<N>(u, plane, 1);
+    if (h.coded) store_planes<N>(u, plane, 1, h.maxprec);
     return emit_block<8 * sizeof(U), N>(out, h, plane, 1);
   } else {
     WideCode<S> wc;

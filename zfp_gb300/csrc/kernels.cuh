@@ -180,6 +180,13 @@ __host__ __device__ constexpr uint32_t img_phys(uint32_t w) { return w + (w >> 4
 __host__ __device__ constexpr uint32_t img_cap(uint32_t phys) { return (uint32_t)((uint64_t)phys * 16 / 17); }
 
 
+// atomic OR of a 64-bit word as two 32-bit atomics (the 32-bit ones are
+// native shared-memory operations), skipping empty halves
+__device__ __forceinline__ void or_shared(uint64_t* p, uint64_t v) {
+  if ((uint32_t)v) atomicOr((unsigned*)p, (unsigned)v);
+  if (v >> 32) atomicOr((unsigned*)p + 1, (unsigned)(v >> 32));
+}
+
 struct SmemSink {
   uint64_t* buf;
   uint32_t word;
@@ -196,7 +203,7 @@ struct SmemSink {
       return;
     }
     if (first) {
-      atomicOr((unsigned long long*)&buf[img_phys(word)], (unsigned long long)w);
+      or_shared(&buf[img_phys(word)], w);
       first = false;
     } else {
       buf[img_phys(word)] = w;
@@ -228,7 +235,7 @@ struct SmemSink {
   }
   __device__ __forceinline__ void finish() {
     if (!fill) return;
-    if (word < cap) atomicOr((unsigned long long*)&buf[img_phys(word)], (unsigned long long)acc);
+    if (word < cap) or_shared(&buf[img_phys(word)], acc);
     else atomicOr(status, (unsigned)kStatusOverflow);
   }
 };
@@ -239,17 +246,17 @@ struct SmemSink {
 // bits past it are dropped and flagged.
 struct ImgOr {
   uint64_t* buf;
-  uint64_t start;     // block's first bit in the image
+  uint32_t start;     // block's first bit in the image
   uint32_t cap;
   unsigned* status;
   __device__ __forceinline__ void or32(uint32_t w, unsigned v) {
     atomicOr((unsigned*)buf + 2 * img_phys(w >> 1) + (w & 1), v);
   }
   // v must have no bits at or above n (n <= 64)
-  __device__ __forceinline__ void set(uint64_t pos, uint64_t v, unsigned n) {
-    const uint64_t a = start + pos;
-    const uint32_t w = (uint32_t)(a >> 5);
-    const unsigned o = (unsigned)(a & 31);
+  __device__ __forceinline__ void set(uint32_t pos, uint64_t v, unsigned n) {
+    const uint32_t a = start + pos;
+    const uint32_t w = a >> 5;
+    const unsigned o = a & 31;
     const unsigned end = o + n;                  // bits spanned from the first 32-bit word
     if ((uint64_t)w + (end + 31) / 32 > 2ull * cap) {   // 32-bit words past the image
       atomicOr(status, (unsigned)kStatusOverflow);
@@ -414,7 +421,7 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
     if constexpr (N <= 64) {
       U u[N];
       prepare_coeffs<S, D, kSel>(h, p, raw, u);
-      if (h.coded) store_planes<N>(u, my_planes, kTile);
+      if (h.coded) store_planes<N>(u, my_planes, kTile, h.maxprec);
       len = fixed ? job.maxbits : block_bits<P, N>(h, my_planes, kTile);
     } else {
       prepare_coeffs<S, D, kSel>(wc.h, p, raw, wc.u);
