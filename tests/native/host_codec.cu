@@ -160,7 +160,7 @@ uint64_t decompress_t(const Geom& g, const zg::BlockParams& p, void* data, const
             ((B*)data)[off] = raw[x + 4 * y + 16 * z + 64 * w];
           }
   }
-  return in.at;
+  return in.tell();
 }
 
 template <typename S>

@@ -678,26 +678,19 @@ ZG_HD unsigned decode_planes(Source& in, unsigned budget, unsigned maxprec, Plan
     uint64_t x = in.read(m);
     bits -= m;
     while (bits && n < (unsigned)N) {
-      // group-test bit plus at most min(bits - 1, N - 1 - n) scan bits
-      unsigned cap = N - 1 - n;
-      if (cap > bits - 1) cap = bits - 1;
-      const uint64_t w = in.peek(cap + 1);
+      const uint64_t w = in.peek64();
       if (!(w & 1)) {          // negative test: rest of the plane is zero
         in.skip(1);
         bits--;
         break;
       }
-      const uint64_t scan = w >> 1;
-      unsigned z;
-      if (scan) {
-        z = ctz64(scan);
-        in.skip(z + 2);
-        bits -= z + 2;
-      } else {
-        z = cap;
-        in.skip(cap + 1);
-        bits -= cap + 1;
-      }
+      // group-test bit plus at most cap = min(bits - 1, N - 1 - n) scan
+      // bits; a sentinel at the limit stops the count of trailing zeros
+      const unsigned cap = N - 1 - n < bits - 1 ? N - 1 - n : bits - 1;
+      const unsigned z = ctz64((w >> 1) | (uint64_t(1) << cap));
+      const unsigned adv = z + (z < cap ? 2u : 1u);   // a found one is consumed; at the limit it is implied
+      in.skip(adv);
+      bits -= adv;
       n += z;
       x |= uint64_t(1) << n;
       n++;
@@ -1327,10 +1320,9 @@ template <bool kGlobal>
 struct WordSourceT {
   const uint64_t* base;
   uint64_t cap;     // readable words
-  uint64_t at;      // absolute position of the next bit
-  uint64_t next;    // index of the next word to load
+  uint64_t next;    // index of the next word to load; the current position is (next - 2) * 64 + pos
   uint64_t lo, hi;
-  unsigned pos;     // bit offset of `at` inside lo
+  unsigned pos;     // bit offset of the current position inside lo
 
   ZG_HD uint64_t load(uint64_t i) const {
 #if defined(__CUDA_ARCH__)
@@ -1341,20 +1333,17 @@ struct WordSourceT {
     return i < cap ? base[i] : 0ull;
 #endif
   }
+  ZG_HD uint64_t tell() const { return (next - 2) * 64 + pos; }
   ZG_HD void seek(uint64_t bit) {
-    at = bit;
     const uint64_t w = bit >> 6;
     lo = load(w);
     hi = load(w + 1);
     next = w + 2;
     pos = (unsigned)(bit & 63);
   }
-  ZG_HD uint64_t peek(unsigned n) const {     // n <= 64
-    const uint64_t w = pos ? (lo >> pos) | (hi << (64 - pos)) : lo;
-    return low_bits(w, n);
-  }
+  ZG_HD uint64_t peek64() const { return pos ? (lo >> pos) | (hi << (64 - pos)) : lo; }
+  ZG_HD uint64_t peek(unsigned n) const { return low_bits(peek64(), n); }   // n <= 64
   ZG_HD void skip(unsigned n) {               // n <= 64
-    at += n;
     pos += n;
     if (pos >= 64) {
       lo = hi;
@@ -1367,7 +1356,7 @@ struct WordSourceT {
     skip(n);
     return v;
   }
-  ZG_HD void skip_long(uint64_t n) { seek(at + n); }
+  ZG_HD void skip_long(uint64_t n) { seek(tell() + n); }
 };
 
 using WordSource = WordSourceT<true>;

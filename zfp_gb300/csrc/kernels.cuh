@@ -517,14 +517,14 @@ __device__ __forceinline__ void decode_tile(const Job& job, uint32_t gt, uint64_
     in.cap = nwords;
     in.seek(start - (w0 << 6));
     decode_block<S, D, kSel>(in, p, raw, pb);
-    end = in.at + (w0 << 6);
+    end = in.tell() + (w0 << 6);
   } else {
     WordSource in;
     in.base = job.words;
     in.cap = job.cap_words;
     in.seek(start);
     decode_block<S, D, kSel>(in, p, raw, pb);
-    end = in.at;
+    end = in.tell();
   }
   if ((job.flags & kVerify) && end != expect) atomicOr(&job.result->status, (unsigned)kStatusIndex);
   scatter<B, D>(job, b, raw);
@@ -601,11 +601,11 @@ __global__ void parse_kernel(const __grid_constant__ Job job) {
   in.cap = job.cap_words;
   in.seek(job.bit0);
   for (uint64_t b = 0; b < job.nblocks; b++) {
-    job.offsets[b] = in.at;
+    job.offsets[b] = in.tell();
     B raw[N];
     decode_block<S, D>(in, p, raw);
   }
-  job.result->end_bit = in.at;
+  job.result->end_bit = in.tell();
 }
 
 }  // namespace zg
