@@ -574,8 +574,8 @@ __global__ void __launch_bounds__(kTile) encode_kernel(const __grid_constant__ J
 // img_words: shared memory for staging a tile's stream words; tiles that do
 // not fit are read from the stream directly
 template <typename S, int D, bool kMulti, int kSel>
-__global__ void __launch_bounds__(kTile) decode_kernel(const __grid_constant__ Job one, const Job* jobs, int njobs,
-                                                       uint32_t total_tiles, uint32_t img_words) {
+__device__ __forceinline__ void decode_body(const Job& one, const Job* jobs, int njobs, uint32_t total_tiles,
+                                            uint32_t img_words) {
   extern __shared__ uint64_t smem_img[];
   uint64_t* img = smem_img;
   uint64_t* planes = smem_img + img_words;
@@ -585,6 +585,21 @@ __global__ void __launch_bounds__(kTile) decode_kernel(const __grid_constant__ J
     decode_tile<S, D, kSel>(*job, gt, img, img_words, planes);
     __syncthreads();
   }
+}
+
+template <typename S, int D, bool kMulti, int kSel>
+__global__ void __launch_bounds__(kTile) decode_kernel(const __grid_constant__ Job one, const Job* jobs, int njobs,
+                                                       uint32_t total_tiles, uint32_t img_words) {
+  decode_body<S, D, kMulti, kSel>(one, jobs, njobs, total_tiles, img_words);
+}
+
+// The same decoder held to three CTAs per SM (168 registers).  Used for
+// 64-bit lossy blocks, where the compiler's own choice (about 180 registers,
+// two CTAs) leaves the SM short of warps: measured 10-17% faster.
+template <typename S, int D, bool kMulti, int kSel>
+__global__ void __launch_bounds__(kTile, 3) decode_kernel_occ3(const __grid_constant__ Job one, const Job* jobs,
+                                                               int njobs, uint32_t total_tiles, uint32_t img_words) {
+  decode_body<S, D, kMulti, kSel>(one, jobs, njobs, total_tiles, img_words);
 }
 
 // Recover block offsets of a variable-rate stream that carries no index by

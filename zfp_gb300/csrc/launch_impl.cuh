@@ -70,7 +70,8 @@ template <typename S, int D, class F>
 static auto with_decoder(const LaunchArgs& a, F&& f) {
   if (a.jobs) return f(KernelTag<decode_kernel<S, D, true, kAnyMode>>{});
   if (a.one.minexp < kMinExp) return f(KernelTag<decode_kernel<S, D, false, kRevOnly>>{});
-  return f(KernelTag<decode_kernel<S, D, false, kLossyOnly>>{});
+  if constexpr (sizeof(S) == 8 && D <= 3) return f(KernelTag<decode_kernel_occ3<S, D, false, kLossyOnly>>{});
+  else return f(KernelTag<decode_kernel<S, D, false, kLossyOnly>>{});
 }
 
 template <typename S, int D>
