@@ -66,12 +66,30 @@ static auto with_encoder(const LaunchArgs& a, F&& f) {
   if (a.one.minexp < kMinExp) return f(KernelTag<encode_kernel<S, D, false, kRevOnly>>{});
   return f(KernelTag<encode_kernel<S, D, false, kLossyOnly>>{});
 }
+// A 32-bit fixed-rate tile small enough for a fifth of an SM's shared memory
+// (with the bit planes) goes to the five-CTA decoder.  Decided from the job
+// alone, so planning and launching pick the same kernel.
+template <typename S, int D>
+static bool five_ctas(const Job& j) {
+  if constexpr (sizeof(S) != 4 || D > 3) {
+    return false;
+  } else {
+    constexpr size_t kShare = 228 * 1024 / 5 - 2048;   // per CTA, less reserved and static memory
+    const size_t tile = image_words((uint64_t)kTile * j.maxbits / 64 + 4) * 8 + plane_smem_bytes<S, D, false>();
+    return (j.flags & kFixedRate) && tile <= kShare;
+  }
+}
+
 template <typename S, int D, class F>
 static auto with_decoder(const LaunchArgs& a, F&& f) {
   if (a.jobs) return f(KernelTag<decode_kernel<S, D, true, kAnyMode>>{});
   if (a.one.minexp < kMinExp) return f(KernelTag<decode_kernel<S, D, false, kRevOnly>>{});
-  if constexpr (sizeof(S) == 8 && D <= 3) return f(KernelTag<decode_kernel_occ3<S, D, false, kLossyOnly>>{});
-  else return f(KernelTag<decode_kernel<S, D, false, kLossyOnly>>{});
+  if constexpr (sizeof(S) == 8 && D <= 3) {
+    return f(KernelTag<decode_kernel_occ<S, D, false, kLossyOnly, 3>>{});
+  } else {
+    if (five_ctas<S, D>(a.one)) return f(KernelTag<decode_kernel_occ<S, D, false, kLossyOnly, 5>>{});
+    return f(KernelTag<decode_kernel<S, D, false, kLossyOnly>>{});
+  }
 }
 
 template <typename S, int D>
