@@ -117,12 +117,11 @@ uint64_t compress_t(const Geom& g, const zg::BlockParams& p, const void* data, u
         zg::BlockHead h;
         U u[N];
         uint64_t plane[P];
-        uint16_t base[P];
         zg::prepare_coeffs<S, D>(h, p, raw, u);
         if (h.coded) zg::store_planes<N>(u, plane, 1, h.maxprec);
         OrSink os{words, out.pos};
         const uint64_t at = out.pos;
-        const unsigned bits = zg::emit_block_2p<P, N>(out, os, h, plane, 1, base, 1);
+        const unsigned bits = zg::emit_block_2p<P, N>(out, os, h, plane, 1);
         if (os.hi > bits || out.pos != at + bits) g_or_overrun = true;
         continue;
       }

@@ -1149,24 +1149,24 @@ ZG_HD unsigned emit_block(Sink& out, const BlockHead& h, const uint64_t* plane, 
 //    and, if anything above n is set, the opening positive group test; the
 //    rest of the plane's code is skipped (pad) and filled in by pass 2.
 //    Planes with such bits ("event planes") are remembered: the slot of
-//    plane k is overwritten with r = x >> n and base[k] receives the
-//    position of its opening test;
+//    plane k is overwritten with r = x >> n;
 //  pass 2, one flat loop over every one bit of every event plane, through
 //    the positional sink `pos` (out.set(at, v, n): OR v, n bits, at the
-//    block-relative bit `at`): the j-th one at offset p of r sits at
-//    base + p + j + 1 and, unless it is the plane's last one, is followed by
-//    a positive test at base + p + j + 2; a last one at the last coefficient
-//    is implied and not written.
+//    block-relative bit `at`).  n changes only at event planes, so the
+//    planes between two event planes each take n + 1 bits (n once all
+//    coefficients are significant) and an event plane's start and length
+//    follow from r alone: pass 2 walks the event planes with no stored
+//    offsets.  The j-th one at offset p of r sits at start + n + 1 + p + j
+//    and, unless it is the plane's last one, is followed by a positive test;
+//    a last one at the last coefficient is implied and not written.
 // Zeros need no writes, and bits at or past the budget are dropped, which
 // cuts the code exactly where the reference's bit budget stops the coder
 // (src/template/encode.c:92-256).  Pass 2 runs once per event of the block
 // rather than once per event inside a loop per plane, so the lanes of a warp
 // diverge far less.  Returns the block's bits, as emit_block.
 template <int P, int N, class Seq, class Pos>
-ZG_HD unsigned emit_block_2p(Seq& seq, Pos& pos, const BlockHead& h, uint64_t* plane, int stride, uint16_t* base,
-                             int bstride) {
+ZG_HD unsigned emit_block_2p(Seq& seq, Pos& pos, const BlockHead& h, uint64_t* plane, int stride) {
   using Mask = typename std::conditional<(P <= 32), uint32_t, uint64_t>::type;
-  constexpr unsigned kImplied = 0x8000;   // base flag: the plane's last one is the implied last coefficient
   seq.put(h.hdr, h.hdr_bits);
   unsigned bits = h.hdr_bits;
   Mask events = 0;                        // bit k: plane k has ones above its n
@@ -1175,7 +1175,7 @@ ZG_HD unsigned emit_block_2p(Seq& seq, Pos& pos, const BlockHead& h, uint64_t* p
   if (h.coded) {
     const int kmin = (unsigned)P > h.maxprec ? P - (int)h.maxprec : 0;
     const uint64_t lim64 = (uint64_t)h.hdr_bits + h.budget;  // first dropped position
-    lim = lim64 < 0x7fffu ? (unsigned)lim64 : 0x7fffu;
+    lim = lim64 < 0xffffu ? (unsigned)lim64 : 0xffffu;
     unsigned at = h.hdr_bits;                                // start of the current plane's code
     unsigned n = 0;
     for (int k = P - 1; k >= kmin && at < lim; k--) {
@@ -1188,7 +1188,6 @@ ZG_HD unsigned emit_block_2p(Seq& seq, Pos& pos, const BlockHead& h, uint64_t* p
       seq.put(low_bits(x, m) | ((uint64_t)ev << m), m + ev);
       if (ev) {
         plane[k * stride] = x >> n0;
-        base[k * bstride] = (uint16_t)((at + n0) | (n == (unsigned)N ? kImplied : 0u));
         events |= Mask(1) << k;
       }
       seq.pad(room - m - ev);
@@ -1202,23 +1201,28 @@ ZG_HD unsigned emit_block_2p(Seq& seq, Pos& pos, const BlockHead& h, uint64_t* p
   }
   seq.finish();
   uint64_t r = 0;
-  unsigned b = 0;
+  unsigned at = h.hdr_bits, n = 0, b = 0;   // at: start of the plane below the last event plane
+  int kprev = P;
   bool implied = false;
   while (r || events) {
     if (!r) {
       const int k = 63 - clz64((uint64_t)events);
       events &= ~(Mask(1) << k);
+      at += (unsigned)(kprev - 1 - k) * (n < (unsigned)N ? n + 1 : n);   // planes without events
+      kprev = k;
       r = plane[k * stride];
-      const unsigned v = base[k * bstride];
-      b = (v & (kImplied - 1)) + 1;     // the j-th one at offset p sits at b + p + j
-      implied = v & kImplied;
+      const unsigned top = n + 64 - (unsigned)clz64(r);              // n after this plane
+      b = at + n + 1;                                                // the j-th one at offset p sits at b + p + j
+      implied = top >= (unsigned)N;
+      at += top + (unsigned)popc64(r) + (implied ? 0u : 1u) - (implied ? 1u : 0u);
+      n = top;
     }
-    const unsigned at = b + ctz64(r);
+    const unsigned p = b + ctz64(r);
     r &= r - 1;
     b++;
-    if (at < lim) {
-      if (r) pos.set(at, at + 1 < lim ? 3 : 1, at + 1 < lim ? 2 : 1);   // the one, then a positive test
-      else if (!implied) pos.set(at, 1, 1);                             // the plane's last one
+    if (p < lim) {
+      if (r) pos.set(p, p + 1 < lim ? 3 : 1, p + 1 < lim ? 2 : 1);   // the one, then a positive test
+      else if (!implied) pos.set(p, 1, 1);                          // the plane's last one
     }
   }
   return bits;

@@ -447,7 +447,7 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
     if constexpr (N <= 64) {
       SmemSink seq{img, excl >> 6, excl & 63u, 0ull, true, nw, &job.result->status};
       ImgOr pos{img, excl, nw, &job.result->status};
-      emit_block_2p<P, N>(seq, pos, h, my_planes, kTile, (uint16_t*)(planes + P * kTile) + threadIdx.x, kTile);
+      emit_block_2p<P, N>(seq, pos, h, my_planes, kTile);
     } else {
       SmemSink out{img, excl >> 6, excl & 63u, 0ull, true, nw, &job.result->status};
       wc.emit(out);
@@ -462,11 +462,10 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
   if (threadIdx.x == 0 && lt + 1 == job.ntiles) job.result->end_bit = G + total;
 }
 
-// dynamic shared memory for the bit planes of one tile (1-3D blocks); the
-// encoder also keeps a 16-bit code position per plane
+// dynamic shared memory for the bit planes of one tile (1-3D blocks)
 template <typename S, int D, bool kEncode>
 constexpr size_t plane_smem_bytes() {
-  return (1 << (2 * D)) <= 64 ? (size_t)8 * sizeof(typename Traits<S>::UInt) * kTile * (kEncode ? 10 : 8) : 0;
+  return (1 << (2 * D)) <= 64 ? (size_t)8 * sizeof(typename Traits<S>::UInt) * kTile * 8 : 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -594,8 +593,9 @@ __global__ void __launch_bounds__(kTile) decode_kernel(const __grid_constant__ J
 }
 
 // The same decoder held to more CTAs per SM.  Three (168 registers) for
-// 64-bit lossy blocks, where the compiler's own choice (about 180 registers,
-// two CTAs) leaves the SM short of warps: measured 10-17% faster.  Five (96
+// 64-bit lossy blocks and 32-bit reversible blocks, where the compiler's own
+// choice (about 180 registers, two CTAs) leaves the SM short of warps:
+// measured 10-17% faster on the former.  Five (96
 // registers) for 32-bit fixed-rate blocks whose tile fits the smaller
 // shared-memory share: measured 10% faster at rate 8.
 template <typename S, int D, bool kMulti, int kSel, int kMinCtas>

@@ -42,8 +42,7 @@ inline uint64_t image_words(uint64_t logical) { return logical + logical / 16 + 
 // instead (GB300 allows 227 KB of shared memory per CTA, static included)
 constexpr size_t kMaxTileSmem = 216 * 1024;
 
-// shared memory the encoder keeps for bit planes and their code positions:
-// 1-3D blocks only (the decoder needs less)
-inline size_t plane_bytes(size_t esize, int dims) { return dims <= 3 ? esize * 8 * kTile * 10 : 0; }
+// shared memory the kernels keep for bit planes: 1-3D blocks only
+inline size_t plane_bytes(size_t esize, int dims) { return dims <= 3 ? esize * 8 * kTile * 8 : 0; }
 
 }  // namespace zg
