@@ -551,9 +551,9 @@ __device__ __forceinline__ const Job* resolve_job(const Job& one, const Job* job
 }
 
 template <typename S, int D, bool kMulti, int kSel>
-__global__ void __launch_bounds__(kTile) encode_kernel(const __grid_constant__ Job one, const Job* jobs, int njobs,
-                                                       LaunchScratch sc, uint32_t total_tiles, int use_ticket,
-                                                       uint64_t* gimg, uint32_t slot_words, uint32_t img_words) {
+__device__ __forceinline__ void encode_body(const Job& one, const Job* jobs, int njobs, const LaunchScratch& sc,
+                                            uint32_t total_tiles, int use_ticket, uint64_t* gimg,
+                                            uint32_t slot_words, uint32_t img_words) {
   extern __shared__ uint64_t smem_img[];
   uint64_t* gslot = gimg ? gimg + (size_t)blockIdx.x * slot_words : nullptr;
   uint64_t* planes = smem_img + img_words;
@@ -568,6 +568,22 @@ __global__ void __launch_bounds__(kTile) encode_kernel(const __grid_constant__ J
     encode_tile<S, D, kSel>(*job, sc, gt, smem_img, img_words, gslot, slot_words, planes);
     __syncthreads();
   }
+}
+
+template <typename S, int D, bool kMulti, int kSel>
+__global__ void __launch_bounds__(kTile) encode_kernel(const __grid_constant__ Job one, const Job* jobs, int njobs,
+                                                       LaunchScratch sc, uint32_t total_tiles, int use_ticket,
+                                                       uint64_t* gimg, uint32_t slot_words, uint32_t img_words) {
+  encode_body<S, D, kMulti, kSel>(one, jobs, njobs, sc, total_tiles, use_ticket, gimg, slot_words, img_words);
+}
+
+// The same encoder held to more CTAs per SM (see decode_kernel_occ).
+template <typename S, int D, bool kMulti, int kSel, int kMinCtas>
+__global__ void __launch_bounds__(kTile, kMinCtas) encode_kernel_occ(const __grid_constant__ Job one, const Job* jobs,
+                                                                     int njobs, LaunchScratch sc, uint32_t total_tiles,
+                                                                     int use_ticket, uint64_t* gimg,
+                                                                     uint32_t slot_words, uint32_t img_words) {
+  encode_body<S, D, kMulti, kSel>(one, jobs, njobs, sc, total_tiles, use_ticket, gimg, slot_words, img_words);
 }
 
 // img_words: shared memory for staging a tile's stream words; tiles that do

@@ -60,14 +60,8 @@ template <auto K> struct KernelTag { static constexpr auto kernel = K; };
 
 // kernel variant: device job array -> multi-job kernel carrying both mode
 // paths; a single job -> the variant of its mode only
-template <typename S, int D, class F>
-static auto with_encoder(const LaunchArgs& a, F&& f) {
-  if (a.jobs) return f(KernelTag<encode_kernel<S, D, true, kAnyMode>>{});
-  if (a.one.minexp < kMinExp) return f(KernelTag<encode_kernel<S, D, false, kRevOnly>>{});
-  return f(KernelTag<encode_kernel<S, D, false, kLossyOnly>>{});
-}
 // A 32-bit fixed-rate tile small enough for a fifth of an SM's shared memory
-// (with the bit planes) goes to the five-CTA decoder.  Decided from the job
+// (with the bit planes) goes to the five-CTA kernels.  Decided from the job
 // alone, so planning and launching pick the same kernel.
 template <typename S, int D>
 static bool five_ctas(const Job& j) {
@@ -78,6 +72,14 @@ static bool five_ctas(const Job& j) {
     const size_t tile = image_words((uint64_t)kTile * j.maxbits / 64 + 4) * 8 + plane_smem_bytes<S, D, false>();
     return (j.flags & kFixedRate) && tile <= kShare;
   }
+}
+
+template <typename S, int D, class F>
+static auto with_encoder(const LaunchArgs& a, F&& f) {
+  if (a.jobs) return f(KernelTag<encode_kernel<S, D, true, kAnyMode>>{});
+  if (a.one.minexp < kMinExp) return f(KernelTag<encode_kernel<S, D, false, kRevOnly>>{});
+  if (five_ctas<S, D>(a.one)) return f(KernelTag<encode_kernel_occ<S, D, false, kLossyOnly, 5>>{});
+  return f(KernelTag<encode_kernel<S, D, false, kLossyOnly>>{});
 }
 
 template <typename S, int D, class F>
