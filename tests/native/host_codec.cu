@@ -7,6 +7,8 @@
 #include <cstring>
 
 #include "../../zfp_gb300/csrc/codec.cuh"
+#include "../../zfp_gb300/csrc/kernels.cuh"
+#include "../../zfp_gb300/csrc/launch.h"
 
 namespace {
 
@@ -239,4 +241,16 @@ extern "C" int zgh_bfp_exact32(const uint32_t* raw, int emax, int special) {
   uint32_t b[64];
   for (int i = 0; i < 64; i++) b[i] = raw[i];
   return zg::bfp_exact<float, 64>(b, emax, special != 0);
+}
+
+// shared-memory image layout (kernels.cuh / launch.h): every logical word
+// of a buffer sized by image_words() lands inside it, for all sizes up to n
+extern "C" int zgh_image_layout_ok(uint32_t n) {
+  for (uint32_t logical = 1; logical <= n; logical++) {
+    const uint32_t phys = (uint32_t)zg::image_words(logical);
+    if (zg::img_cap(phys) < logical) return 0;
+    if (zg::img_phys(zg::img_cap(phys) - 1) >= phys) return 0;
+    if (zg::img_phys(logical - 1) >= phys) return 0;
+  }
+  return 1;
 }

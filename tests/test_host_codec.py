@@ -24,7 +24,7 @@ def host():
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.exists(nvcc):
         pytest.skip("nvcc not available")
-    deps = [SRC, os.path.join(HERE, "..", "zfp_gb300", "csrc", "codec.cuh")]
+    deps = [SRC] + [os.path.join(HERE, "..", "zfp_gb300", "csrc", f) for f in ("codec.cuh", "kernels.cuh", "launch.h")]
     if not os.path.exists(OUT) or any(os.path.getmtime(d) > os.path.getmtime(OUT) for d in deps):
         os.makedirs(os.path.dirname(OUT), exist_ok=True)
         subprocess.run([nvcc, "-std=c++17", "-O2", "-shared", "-Xcompiler", "-fPIC", "-o", OUT, SRC], check=True)
@@ -163,3 +163,9 @@ def test_bfp_exactness_shortcut(host):
             assert got == want, (dtype, em, trial)
             seen.add(want)
         assert seen == {True, False}
+
+
+def test_shared_memory_image_layout(host):
+    """Tile images keep a spare word after every 16 (bank spreading); a buffer
+    sized for L logical words holds them all, and nothing maps past its end."""
+    assert host.zgh_image_layout_ok(C.c_uint32(200000))
