@@ -21,6 +21,7 @@
 // include/zfp/bitstream.inl:226-313 (64-bit words, LSB first).
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <type_traits>
@@ -241,6 +242,16 @@ template <typename S> ZG_HD typename Traits<S>::Int trunc_int(S x) {
 #endif
 }
 
+// truncation toward zero, in the same format
+template <typename S> ZG_HD S ftrunc(S x) {
+#if defined(__CUDA_ARCH__)
+  if constexpr (sizeof(S) == 4) return truncf(x);
+  else return trunc(x);
+#else
+  return std::trunc(x);
+#endif
+}
+
 // round-to-nearest integer -> float of the same width
 template <typename S> ZG_HD S int_to_float(typename Traits<S>::Int i) {
 #if defined(__CUDA_ARCH__)
@@ -412,11 +423,24 @@ ZG_HD bool bfp_exact(const typename Traits<S>::Bits (&raw)[N], int emax, bool sp
   const int lo = emax - (T::kPrec - 2);
   bool exact = true;
   if (!special && lo >= 1 - T::kEBias) {
+    if constexpr (sizeof(S) == 4) {
+      // float: on the FP32 pipe.  x * 2^(P-2-emax) is exact unless it falls
+      // below the normal range, and is then nonzero only if it is not an
+      // integer; a value that vanishes there (y == 0, x != 0) is not exact.
+      const S s = pow2<S>(T::kPrec - 2 - emax);
 #pragma unroll (N <= 64 ? N : 1)
-    for (int i = 0; i < N; i++) {
-      int q;
-      const B m = significand<S>(raw[i], q);
-      exact &= m ? q + (int)ctz64((uint64_t)m) >= lo : raw[i] == 0;
+      for (int i = 0; i < N; i++) {
+        const S y = fmul<S>(s, from_bits<S>(raw[i]));
+        const bool zero = (B)(raw[i] << 1) == 0;
+        exact &= zero ? raw[i] == 0 : (y == ftrunc<S>(y)) & (y != S(0));
+      }
+    } else {
+#pragma unroll (N <= 64 ? N : 1)
+      for (int i = 0; i < N; i++) {
+        int q;
+        const B m = significand<S>(raw[i], q);
+        exact &= m ? q + (int)ctz64((uint64_t)m) >= lo : raw[i] == 0;
+      }
     }
   } else {
     const S s = pow2<S>(T::kPrec - 2 - emax), r = pow2<S>(lo);
@@ -1108,7 +1132,13 @@ ZG_HD unsigned block_bits(const BlockHead& h, const uint64_t* plane, int stride)
   if (h.coded) {
     const int kmin = (unsigned)P > h.maxprec ? P - (int)h.maxprec : 0;
     unsigned n = 0, code = 0;
-    for (int k = P - 1; k >= kmin && code < h.budget; k--) code += plane_bits<N>(plane[k * stride], n);
+    for (int k = P - 1; k >= kmin && code < h.budget; k--) {
+      if (n >= (unsigned)N) {                 // all coefficients significant: N verbatim bits per plane
+        code += (unsigned)(k - kmin + 1) * N;
+        break;
+      }
+      code += plane_bits<N>(plane[k * stride], n);
+    }
     bits += code < h.budget ? code : h.budget;
   }
   return bits > h.pad_to ? bits : h.pad_to;
@@ -1178,7 +1208,8 @@ ZG_HD unsigned emit_block_2p(Seq& seq, Pos& pos, const BlockHead& h, uint64_t* p
     lim = lim64 < 0xffffu ? (unsigned)lim64 : 0xffffu;
     unsigned at = h.hdr_bits;                                // start of the current plane's code
     unsigned n = 0;
-    for (int k = P - 1; k >= kmin && at < lim; k--) {
+    int k = P - 1;
+    for (; k >= kmin && at < lim && n < (unsigned)N; k--) {
       const uint64_t x = plane[k * stride];
       const unsigned n0 = n;
       const unsigned len = plane_bits<N>(x, n);
@@ -1192,6 +1223,12 @@ ZG_HD unsigned emit_block_2p(Seq& seq, Pos& pos, const BlockHead& h, uint64_t* p
       }
       seq.pad(room - m - ev);
       at += len;
+    }
+    // once every coefficient is significant a plane is its N bits, verbatim
+    for (; k >= kmin && at < lim; k--) {
+      const unsigned m = lim - at < (unsigned)N ? lim - at : (unsigned)N;
+      seq.put(low_bits(plane[k * stride], m), m);
+      at += N;
     }
     bits += (at < lim ? at : lim) - h.hdr_bits;
   }

@@ -376,15 +376,28 @@ __device__ __forceinline__ void write_tile(const Job& job, const LaunchScratch& 
   const uint64_t hw = G >> 6, tw = E >> 6;
   const unsigned sh = (unsigned)(G & 63), te = (unsigned)(E & 63);
   const bool first = lt == 0, last = lt + 1 == job.ntiles;
-  const uint64_t wend = te ? tw + 1 : tw;
-  for (uint64_t w = hw + threadIdx.x; w < wend; w += kTile) {
-    const uint64_t j = w - hw;
-    const uint64_t cur = j < nimg ? img[img_phys((uint32_t)j)] : 0ull;
-    const uint64_t prev = j && j - 1 < nimg ? img[img_phys((uint32_t)j - 1)] : 0ull;
+  const uint32_t cnt = (uint32_t)((te ? tw + 1 : tw) - hw);   // stream words this tile touches
+  const bool in_bounds = hw + cnt <= job.cap_words;
+  const unsigned lane = threadIdx.x & 31;
+  // whole warps step through the words so the word below comes from the
+  // neighbouring lane; lane 0 reads its own
+  for (uint32_t base = threadIdx.x - lane; base < cnt; base += kTile) {
+    const uint32_t j = base + lane;
+    const uint64_t cur = j < nimg ? img[img_phys(j)] : 0ull;
+    uint64_t prev = __shfl_up_sync(0xffffffffu, cur, 1);
+    if (lane == 0) prev = j && j - 1 < nimg ? img[img_phys(j - 1)] : 0ull;
+    if (j >= cnt) continue;
     uint64_t v = sh ? (cur << sh) | (prev >> (64 - sh)) : cur;
-    if (w == hw && first && sh) v |= job.head_word & ((1ull << sh) - 1);
-    if (w == hw && sh && !first) merge_word(job, sc, gt, 1, w, v);
-    else if (w == tw && te && !last) merge_word(job, sc, gt + 1, 0, w, v);
+    const uint64_t w = hw + j;
+    if (j == 0 && sh) {
+      if (first) v |= job.head_word & ((1ull << sh) - 1);
+      else {
+        merge_word(job, sc, gt, 1, w, v);
+        continue;
+      }
+    }
+    if (w == tw && te && !last) merge_word(job, sc, gt + 1, 0, w, v);
+    else if (in_bounds) job.words[w] = v;
     else store_word(job, w, v);
   }
 }

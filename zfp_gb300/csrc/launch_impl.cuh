@@ -78,7 +78,9 @@ template <typename S, int D, class F>
 static auto with_encoder(const LaunchArgs& a, F&& f) {
   if (a.jobs) return f(KernelTag<encode_kernel<S, D, true, kAnyMode>>{});
   if (a.one.minexp < kMinExp) return f(KernelTag<encode_kernel<S, D, false, kRevOnly>>{});
-  if (five_ctas<S, D>(a.one)) return f(KernelTag<encode_kernel_occ<S, D, false, kLossyOnly, 5>>{});
+  if constexpr (sizeof(S) == 4 && D <= 3) {
+    if (five_ctas<S, D>(a.one)) return f(KernelTag<encode_kernel_occ<S, D, false, kLossyOnly, 5>>{});
+  }
   return f(KernelTag<encode_kernel<S, D, false, kLossyOnly>>{});
 }
 
