@@ -638,6 +638,59 @@ ZG_HD void take_planes(const uint64_t (&pl)[P], U (&u)[N]) {
   }
 }
 
+// 32-bit half h (0 = low) of the plane word at p.  The kernels keep planes
+// in shared memory and store halves with 32-bit accesses; the host writes
+// half 0 first, as a whole word.
+ZG_HD void set_half(uint64_t* p, int h, uint32_t v) {
+#if defined(__CUDA_ARCH__)
+  reinterpret_cast<uint32_t*>(p)[h] = v;
+#else
+  if (h) *p |= (uint64_t)v << 32;
+  else *p = v;
+#endif
+}
+
+// coefficients -> planes stored at plane[k * stride].  Each 32x32 transpose
+// (one 32-bit half of 32 coefficients) is stored as soon as it is done, so
+// no array of all planes is held in registers next to the coefficients.
+// 64-bit coefficients whose coded planes all lie in the top half
+// (maxprec <= 32: every lossy mode but high precision) transpose only their
+// high words.
+template <int N, typename U>
+ZG_HD void store_planes(const U (&u)[N], uint64_t* plane, int stride, unsigned maxprec = 8 * sizeof(U)) {
+  constexpr int P = 8 * sizeof(U);
+  if constexpr (N == 4) {
+    uint64_t pl[P];
+    make_planes<N>(u, pl);
+#pragma unroll
+    for (int k = 0; k < P; k++) plane[k * stride] = pl[k];
+  } else {
+    constexpr int G = (N + 31) / 32, H = P / 32;
+    const bool top = P == 64 && maxprec <= 32;
+#pragma unroll
+    for (int half = 0; half < H; half++) {
+      if (top && half == 0) continue;
+#pragma unroll
+      for (int grp = 0; grp < G; grp++) {
+        uint32_t a[32];
+#pragma unroll
+        for (int i = 0; i < 32; i++) {
+          const int c = 32 * grp + i;
+          a[i] = c < N ? (uint32_t)((uint64_t)u[c < N ? c : 0] >> (32 * half)) : 0u;
+        }
+        transpose32(a);
+#pragma unroll
+        for (int k = 0; k < 32; k++) {
+          uint64_t* q = plane + (32 * half + k) * stride;
+          if (G == 1) *q = a[k];
+          else set_half(q, grp, a[k]);
+        }
+      }
+    }
+  }
+}
+
+
 // ---------------------------------------------------------------------------
 // embedded coder for N <= 64 coefficients (one 64-bit word per plane).
 // Every output bit costs one unit of budget; see the header comment.
@@ -1265,29 +1318,6 @@ ZG_HD unsigned emit_block_2p(Seq& seq, Pos& pos, const BlockHead& h, uint64_t* p
   return bits;
 }
 
-// coefficients -> planes stored at plane[k * stride].  64-bit coefficients
-// whose coded planes all lie in the top half (maxprec <= 32: every lossy
-// mode but high precision) transpose only their high words.
-template <int N, typename U>
-ZG_HD void store_planes(const U (&u)[N], uint64_t* plane, int stride, unsigned maxprec = 8 * sizeof(U)) {
-  constexpr int P = 8 * sizeof(U);
-  if constexpr (P == 64 && N > 4) {
-    if (maxprec <= 32) {
-      uint32_t hi[N];
-#pragma unroll
-      for (int i = 0; i < N; i++) hi[i] = (uint32_t)(u[i] >> 32);
-      uint64_t pl[32];
-      make_planes<N>(hi, pl);
-#pragma unroll
-      for (int k = 0; k < 32; k++) plane[(32 + k) * stride] = pl[k];
-      return;
-    }
-  }
-  uint64_t pl[P];
-  make_planes<N>(u, pl);
-#pragma unroll
-  for (int k = 0; k < P; k++) plane[k * stride] = pl[k];
-}
 
 // 4D blocks keep the rolled wide coder over the coefficient array
 template <typename S>

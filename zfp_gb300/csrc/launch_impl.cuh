@@ -77,7 +77,10 @@ static bool five_ctas(const Job& j) {
 template <typename S, int D, class F>
 static auto with_encoder(const LaunchArgs& a, F&& f) {
   if (a.jobs) return f(KernelTag<encode_kernel<S, D, true, kAnyMode>>{});
-  if (a.one.minexp < kMinExp) return f(KernelTag<encode_kernel<S, D, false, kRevOnly>>{});
+  if (a.one.minexp < kMinExp) {
+    if constexpr (sizeof(S) == 8 && D <= 3) return f(KernelTag<encode_kernel_occ<S, D, false, kRevOnly, 3>>{});
+    else return f(KernelTag<encode_kernel<S, D, false, kRevOnly>>{});
+  }
   if constexpr (sizeof(S) == 4 && D <= 3) {
     if (five_ctas<S, D>(a.one)) return f(KernelTag<encode_kernel_occ<S, D, false, kLossyOnly, 5>>{});
   }
