@@ -254,3 +254,43 @@ extern "C" int zgh_image_layout_ok(uint32_t n) {
   }
   return 1;
 }
+
+// block offsets by the length-only decoder (skip_block), as the GPU parse
+// kernel recovers them for streams without an index: ends[b] = first bit
+// after block b
+template <typename S, int D>
+uint64_t parse_t(const Geom& g, const zg::BlockParams& p, const uint64_t* words, uint64_t cap, uint64_t bit0,
+                 uint64_t* ends) {
+  zg::WordSource in;
+  in.base = words;
+  in.cap = cap;
+  in.seek(bit0);
+  for (size_t b = 0; b < g.blocks; b++) {
+    zg::skip_block<S, D>(in, p);
+    ends[b] = in.tell();
+  }
+  return in.tell();
+}
+
+template <typename S>
+uint64_t parse_s(const Geom& g, const zg::BlockParams& p, const uint64_t* w, uint64_t cap, uint64_t b0, uint64_t* e) {
+  switch (g.dims) {
+    case 1: return parse_t<S, 1>(g, p, w, cap, b0, e);
+    case 2: return parse_t<S, 2>(g, p, w, cap, b0, e);
+    case 3: return parse_t<S, 3>(g, p, w, cap, b0, e);
+    default: return parse_t<S, 4>(g, p, w, cap, b0, e);
+  }
+}
+
+extern "C" uint64_t zgh_parse(int type, int dims, const size_t* n, const unsigned* prm, const uint64_t* words,
+                              uint64_t cap, uint64_t bit0, uint64_t* ends) {
+  const ptrdiff_t s[4] = {0, 0, 0, 0};
+  Geom g = geom(dims, n, s);
+  zg::BlockParams p{prm[0], prm[1], prm[2], (int32_t)prm[3]};
+  switch (type) {
+    case 1: return parse_s<int32_t>(g, p, words, cap, bit0, ends);
+    case 2: return parse_s<int64_t>(g, p, words, cap, bit0, ends);
+    case 3: return parse_s<float>(g, p, words, cap, bit0, ends);
+    default: return parse_s<double>(g, p, words, cap, bit0, ends);
+  }
+}

@@ -169,3 +169,32 @@ def test_shared_memory_image_layout(host):
     """Tile images keep a spare word after every 16 (bank spreading); a buffer
     sized for L logical words holds them all, and nothing maps past its end."""
     assert host.zgh_image_layout_ok(C.c_uint32(200000))
+
+
+@pytest.mark.parametrize("dims", [1, 2, 3, 4])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64, np.int32, np.int64], ids=lambda d: np.dtype(d).name)
+def test_length_only_parse_matches_oracle_block_ends(host, oracle, dims, dtype):
+    """skip_block (the GPU parse of streams without an index) ends every
+    block exactly where the oracle's encoder ended it, in every mode."""
+    rng = np.random.default_rng(100 + dims)
+    modes = [("rate", 4), ("rate", 12.5), ("precision", 9), ("precision", 40), ("accuracy", 1e-3),
+             ("accuracy", 1e-9), ("reversible", None), ("expert", (30, 70, 33, -5)), ("expert", (64, 900, 64, -30))]
+    for mode, arg in modes:
+        if mode == "accuracy" and np.dtype(dtype).kind == "i":
+            continue
+        shape = tuple(int(v) for v in rng.integers(1, {1: 60, 2: 17, 3: 10, 4: 7}[dims], size=dims))
+        if np.dtype(dtype).kind == "f":
+            a = (np.cumsum(rng.standard_normal(shape), axis=-1) * 10.0 ** rng.uniform(-5, 5)).astype(dtype)
+            a.flat[:: max(1, a.size // 7)] = 0
+        else:
+            a = rng.integers(-(1 << 20), 1 << 20, size=shape, dtype=dtype)
+        prm = mode_params(mode, arg, dtype, dims)
+        bit0 = int(rng.integers(0, 100))
+        words, end, be = oracle.compress(a, prm, bit0=bit0, block_ends=True)
+        n = (C.c_size_t * 4)(*(list(reversed(a.shape)) + [0] * (4 - dims)))
+        p = (C.c_uint * 4)(*[v & 0xffffffff for v in prm])
+        ends = np.zeros(len(be), dtype=np.uint64)
+        host.zgh_parse.restype = C.c_uint64
+        got = host.zgh_parse(ZTYPE[np.dtype(dtype)], dims, n, p, C.c_void_p(words.ctypes.data),
+                             C.c_uint64(len(words)), C.c_uint64(bit0), C.c_void_p(ends.ctypes.data))
+        assert got == end and np.array_equal(ends, be), (mode, arg, shape)

@@ -1357,6 +1357,95 @@ ZG_HD unsigned encode_block(Sink& out, const BlockParams& p, const typename Trai
   }
 }
 
+// ---------------------------------------------------------------------------
+// Length-only decoding, for recovering block offsets of a variable-rate
+// stream that carries no index: the same bits are consumed as by
+// decode_block, but planes are not formed and nothing is transformed.
+
+// bits of the plane code (the group-test rules of decode_planes and
+// decode_planes_wide, any N), scanning with 64-bit peeks
+template <int N, int P, class Source>
+ZG_HD unsigned skip_planes(Source& in, unsigned budget, unsigned maxprec) {
+  const int kmin = (unsigned)P > maxprec ? P - (int)maxprec : 0;
+  unsigned bits = budget, n = 0;
+  for (int k = P - 1; k >= kmin && bits; k--) {
+    unsigned m = n < bits ? n : bits;        // verbatim bits
+    bits -= m;
+    while (m) {
+      const unsigned c = m < 64 ? m : 64;
+      in.skip(c);
+      m -= c;
+    }
+    while (bits && n < (unsigned)N) {
+      const bool positive = in.peek64() & 1;
+      in.skip(1);
+      bits--;
+      if (!positive) break;                   // rest of the plane is zero
+      // scan at most cap bits for the next one; none: it is implied at the limit
+      const unsigned cap = N - 1 - n < bits ? N - 1 - n : bits;
+      unsigned z = 0;
+      bool found = false;
+      while (z < cap) {
+        const unsigned c = cap - z < 64 ? cap - z : 64;
+        const uint64_t w = in.peek64();
+        const uint64_t sw = c < 64 ? (w | (uint64_t(1) << c)) : w;
+        const unsigned t = sw ? ctz64(sw) : 64u;
+        if (t < c) {
+          in.skip(t + 1);
+          z += t;
+          found = true;
+          break;
+        }
+        in.skip(c);
+        z += c;
+      }
+      bits -= z + (found ? 1u : 0u);
+      n += z + 1;
+    }
+  }
+  return budget - bits;
+}
+
+// bits of a whole block (decode_block's header and padding rules)
+template <typename S, int D, class Source>
+ZG_HD unsigned skip_block(Source& in, const BlockParams& p) {
+  using T = Traits<S>;
+  using U = typename T::UInt;
+  constexpr int N = 1 << (2 * D), P = 8 * sizeof(U);
+  constexpr unsigned kPBits = sizeof(U) == 4 ? 5 : 6;
+  const bool rev = p.minexp < kMinExp;
+  unsigned bits = 0, minbits = p.minbits, maxbits = p.maxbits, maxprec = p.maxprec;
+  if constexpr (T::kFloat) {
+    bits = 1;
+    if (!in.read(1)) {                        // all-zero block
+      if (minbits > bits) { in.skip_long(minbits - bits); bits = minbits; }
+      return bits;
+    }
+    if (rev) {
+      bits++;
+      if (!in.read(1)) {                      // block-floating-point: exponent follows
+        bits += T::kEBits;
+        in.skip(T::kEBits);
+      }
+    } else {
+      bits += T::kEBits;
+      const int emax = (int)in.read(T::kEBits) - T::kEBias;
+      maxprec = coded_precision(emax, p.maxprec, p.minexp, D);
+    }
+    minbits = p.minbits - umin(bits, p.minbits);
+    maxbits = p.maxbits - bits;
+  }
+  unsigned code;
+  if (rev) {
+    const unsigned prec = (unsigned)in.read(kPBits) + 1;
+    code = kPBits + skip_planes<N, P>(in, maxbits - kPBits, prec);
+  } else {
+    code = skip_planes<N, P>(in, maxbits, maxprec);
+  }
+  if (code < minbits) { in.skip_long(minbits - code); code = minbits; }
+  return bits + code;
+}
+
 template <typename S, int D, int kSel = kAnyMode, class Source>
 ZG_HD unsigned decode_block(Source& in, const BlockParams& p, typename Traits<S>::Bits (&raw)[1 << (2 * D)],
                             PlaneBuf pb) {
