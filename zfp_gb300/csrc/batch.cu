@@ -194,7 +194,6 @@ zfp_gb300_batch* zfp_gb300_batch_create(zfp_stream* const* streams, const zfp_fi
           }
           Job pj = j;
           pj.offsets = idx->ptr;
-          pj.block_words = (uint32_t)std::min<uint64_t>(block_bound(fi, z) / 64 + 2, 0xffffffffu);
           if ((e = cudaMemset(j.result, 0, sizeof(JobResult))) != cudaSuccess ||
               (e = launch_parse_any(fi.type, fi.dims, pj, nullptr)) != cudaSuccess ||
               (e = cudaMemcpy(&r, j.result, sizeof r, cudaMemcpyDeviceToHost)) != cudaSuccess) {

@@ -629,7 +629,6 @@ size_t gpu_decompress(zfp_stream* z, zfp_field* f) {
     if (!parsed && !(parsed = make_index(fi.nblocks, st, pe))) return pe;
     Job pj = job;
     pj.offsets = parsed->ptr;
-    pj.block_words = (uint32_t)std::min<uint64_t>(bound / 64 + 2, 0xffffffffu);
     if ((pe = launch_parse_any(fi.type, fi.dims, pj, st)) != cudaSuccess) return pe;
     JobResult r;
     if ((pe = cudaMemcpyAsync(&r, lm.result, sizeof r, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return pe;

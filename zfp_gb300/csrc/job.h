@@ -42,7 +42,7 @@ struct Job {
   uint32_t flags;           // JobFlags
   uint32_t tile0;           // first tile of this job in the launch
   uint32_t ntiles;
-  uint32_t block_words;     // parse: words one block can span (0 = unknown)
+  uint32_t reserved;
   uint64_t* words;          // stream words, index 0 = beginning of the stream buffer
   uint64_t cap_words;       // words addressable at `words`
   uint64_t bit0;            // stream bit where the job's first block starts

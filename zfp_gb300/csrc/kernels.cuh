@@ -637,59 +637,24 @@ __global__ void __launch_bounds__(kTile, kMinCtas) decode_kernel_occ(const __gri
 // Recover block offsets of a variable-rate stream that carries no index by
 // walking it block after block (one thread; used only for streams this
 // library did not write).
-// Block offsets of a variable-rate stream that carries no index.  The chain
-// of block lengths is sequential, so one lane parses (length-only,
-// skip_block) while the warp keeps a window of the stream in shared memory:
-// the lanes stage kParseWin words with coalesced loads, lane 0 parses every
-// block that surely ends inside the window, and the warp moves the window to
-// where lane 0 stopped.  Blocks whose bound is unknown or too large for the
-// window are read from the stream directly.
-constexpr uint32_t kParseWin = 4096;   // logical words (34 KB with the bank spreading)
-
+// Block offsets of a variable-rate stream that carries no index: the chain
+// of block lengths is sequential, so one thread walks it with the
+// length-only decoder (skip_block).  A wider window staged by the warp in
+// shared memory was measured no faster: the walk is bound by its own
+// dependent instructions (about 5 us per 3D block), not by memory.
 template <typename S, int D>
-__global__ void __launch_bounds__(32) parse_kernel(const __grid_constant__ Job job) {
-  __shared__ uint64_t win[kParseWin + kParseWin / 16 + 1];
-  const unsigned lane = threadIdx.x;
+__global__ void parse_kernel(const __grid_constant__ Job job) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const BlockParams p{job.minbits, job.maxbits, job.maxprec, job.minexp};
-  uint64_t pos = job.bit0, b = 0;
-  const bool windowed = job.block_words && job.block_words + 2 < kParseWin / 2;
-  if (!windowed) {
-    if (lane == 0) {
-      WordSource in;
-      in.base = job.words;
-      in.cap = job.cap_words;
-      in.seek(pos);
-      for (; b < job.nblocks; b++) {
-        job.offsets[b] = in.tell();
-        skip_block<S, D>(in, p);
-      }
-      job.result->end_bit = in.tell();
-    }
-    return;
+  WordSource in;
+  in.base = job.words;
+  in.cap = job.cap_words;
+  in.seek(job.bit0);
+  for (uint64_t b = 0; b < job.nblocks; b++) {
+    job.offsets[b] = in.tell();
+    skip_block<S, D>(in, p);
   }
-  while (b < job.nblocks) {
-    const uint64_t w0 = pos >> 6;
-    for (uint32_t i = lane; i < kParseWin; i += 32)
-      win[img_phys(i)] = w0 + i < job.cap_words ? __ldg((const unsigned long long*)job.words + w0 + i) : 0ull;
-    __syncwarp();
-    if (lane == 0) {
-      SharedSource in;
-      in.base = win;
-      in.cap = kParseWin;
-      in.seek(pos - (w0 << 6));
-      // a block starting at word w ends before word w + block_words
-      const uint64_t last_start = (uint64_t)(kParseWin - job.block_words - 2) << 6;
-      for (; b < job.nblocks && in.tell() <= last_start; b++) {
-        job.offsets[b] = in.tell() + (w0 << 6);
-        skip_block<S, D>(in, p);
-      }
-      pos = in.tell() + (w0 << 6);
-    }
-    pos = __shfl_sync(0xffffffffu, pos, 0);
-    b = __shfl_sync(0xffffffffu, b, 0);
-    __syncwarp();
-  }
-  if (lane == 0) job.result->end_bit = pos;
+  job.result->end_bit = in.tell();
 }
 
 }  // namespace zg
