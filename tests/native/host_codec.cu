@@ -55,6 +55,7 @@ struct OrSink {
     if (o && o + n > 64) words[(a >> 6) + 1] |= v >> (64 - o);
     if (pos + n > hi) hi = pos + n;
   }
+  ZG_HD void set_small(uint64_t pos, unsigned v, unsigned n) { set(pos, v, n); }
 };
 
 struct Geom {

@@ -1311,8 +1311,8 @@ ZG_HD unsigned emit_block_2p(Seq& seq, Pos& pos, const BlockHead& h, uint64_t* p
     r &= r - 1;
     b++;
     if (p < lim) {
-      if (r) pos.set(p, p + 1 < lim ? 3 : 1, p + 1 < lim ? 2 : 1);   // the one, then a positive test
-      else if (!implied) pos.set(p, 1, 1);                          // the plane's last one
+      if (r) pos.set_small(p, p + 1 < lim ? 3u : 1u, p + 1 < lim ? 2u : 1u);   // the one, then a positive test
+      else if (!implied) pos.set_small(p, 1u, 1u);                          // the plane's last one
     }
   }
   return bits;

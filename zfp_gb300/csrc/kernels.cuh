@@ -249,23 +249,18 @@ struct ImgOr {
   uint32_t start;     // block's first bit in the image
   uint32_t cap;
   unsigned* status;
-  __device__ __forceinline__ void or32(uint32_t w, unsigned v) {
-    atomicOr((unsigned*)buf + 2 * img_phys(w >> 1) + (w & 1), v);
-  }
-  // v must have no bits at or above n (n <= 64)
-  __device__ __forceinline__ void set(uint32_t pos, uint64_t v, unsigned n) {
+  // one or two bits (v < 4): one 32-bit atomic, two when they straddle words
+  __device__ __forceinline__ void set_small(uint32_t pos, unsigned v, unsigned n) {
     const uint32_t a = start + pos;
-    const uint32_t w = a >> 5;
-    const unsigned o = a & 31;
-    const unsigned end = o + n;                  // bits spanned from the first 32-bit word
-    if ((uint64_t)w + (end + 31) / 32 > 2ull * cap) {   // 32-bit words past the image
+    if (a + n > 64u * cap) {
       atomicOr(status, (unsigned)kStatusOverflow);
       return;
     }
-    const uint64_t lo = v << o;
-    or32(w, (unsigned)lo);
-    if (end > 32) or32(w + 1, (unsigned)(lo >> 32));
-    if (end > 64) or32(w + 2, (unsigned)(v >> (64 - o)));
+    const uint32_t w = a >> 5;
+    const unsigned o = a & 31;
+    unsigned* b = (unsigned*)buf + w + ((w >> 5) << 1);   // 32-bit word w of the bank-spread image
+    atomicOr(b, v << o);
+    if (o + n > 32) atomicOr((unsigned*)buf + (w + 1) + (((w + 1) >> 5) << 1), v >> (32 - o));
   }
 };
 
