@@ -304,3 +304,27 @@ def test_pinned_host_buffers_zero_copy(lib, oracle, cuda):
         r3, _ = zfp_run(lib, "decompress", out2.ctypes.data, zt, n, s, mode, arg, page.ctypes.data, nwords * 8)
         assert r3 == r and lib.zfp_gb300_last_staged_bytes() > 0, msg
         assert np.array_equal(out2.view(np.uint8), ref_out.view(np.uint8)), msg
+
+
+def test_foreign_stream_long_parallel_parse(lib, cuda):
+    """A long variable-rate stream with no index (more than 32,768 blocks)
+    takes the speculative parallel parse; the decoded arrays must equal the
+    ones decoded with the encoder's own index, bit for bit."""
+    torch = cuda
+    from zfp_gb300 import synth
+    for dtype, ztype, shape, mode, arg in [(torch.float32, capi.TYPE_FLOAT, (64, 256, 256), "accuracy", 1e-3),
+                                           (torch.float32, capi.TYPE_FLOAT, (48, 200, 320), "reversible", None),
+                                           (torch.float64, capi.TYPE_DOUBLE, (64, 192, 192), "precision", 30)]:
+        x = synth.smooth_field_torch(shape, dtype, seed=5, noise=1e-2)
+        n, s = tuple(reversed(shape)), (0, 0, 0)
+        cap = x.numel() * x.element_size() * 2 + 4096
+        buf = torch.zeros(cap // 8, dtype=torch.int64, device="cuda")
+        size, _ = zfp_run(lib, "compress", x.data_ptr(), ztype, n, s, mode, arg, buf.data_ptr(), cap)
+        assert size, lib.zfp_gb300_last_error()
+        out_idx = torch.zeros_like(x)
+        assert zfp_run(lib, "decompress", out_idx.data_ptr(), ztype, n, s, mode, arg, buf.data_ptr(), cap)[0] == size
+        foreign = buf.clone()     # another buffer: no recorded index, offsets come from the parse
+        out = torch.zeros_like(x)
+        r, _ = zfp_run(lib, "decompress", out.data_ptr(), ztype, n, s, mode, arg, foreign.data_ptr(), cap)
+        assert r == size, (mode, lib.zfp_gb300_last_error())
+        assert torch.equal(out.view(torch.int8), out_idx.view(torch.int8)), mode

@@ -652,4 +652,99 @@ __global__ void parse_kernel(const __grid_constant__ Job job) {
   job.result->end_bit = in.tell();
 }
 
+// ---------------------------------------------------------------------------
+// Speculative parallel parse.  A wrong start, parsed on, often lands on a
+// true block boundary after a few hundred blocks, and from there on its
+// boundaries are the true ones.  So:
+//  1. parse_probe: one thread parses the first blocks for the mean length;
+//  2. parse_spec: worker w (one thread each) starts at bit0 + w * seg and
+//     records the starts of `k` consecutive blocks and the end of the last;
+//  3. parse_stitch: one thread follows the true chain from bit0.  At a true
+//     position it looks for that exact position among the records of the
+//     workers that cover it; found, it adopts the rest of that worker's
+//     records (all true: the parse is deterministic), else it parses one
+//     block itself and tries again a few blocks later.
+// Every adopted offset therefore follows from a position reached by the
+// true chain: the result is the sequential parse's, only faster.
+
+template <typename S, int D>
+__global__ void parse_probe(const __grid_constant__ Job job, uint32_t count, unsigned long long* mean_bits) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const BlockParams p{job.minbits, job.maxbits, job.maxprec, job.minexp};
+  WordSource in;
+  in.base = job.words;
+  in.cap = job.cap_words;
+  in.seek(job.bit0);
+  for (uint32_t b = 0; b < count; b++) skip_block<S, D>(in, p);
+  *mean_bits = (in.tell() - job.bit0 + count - 1) / count;
+}
+
+template <typename S, int D>
+__global__ void parse_spec(const __grid_constant__ Job job, uint64_t seg, uint32_t k, uint32_t workers,
+                           unsigned long long* rec) {
+  const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= workers) return;
+  const BlockParams p{job.minbits, job.maxbits, job.maxprec, job.minexp};
+  WordSource in;
+  in.base = job.words;
+  in.cap = job.cap_words;
+  in.seek(job.bit0 + (uint64_t)w * seg);
+  unsigned long long* r = rec + (size_t)w * (k + 1);
+  for (uint32_t j = 0; j < k; j++) {
+    r[j] = in.tell();
+    skip_block<S, D>(in, p);
+  }
+  r[k] = in.tell();
+}
+
+// index of `pos` among the k sorted starts r[0..k), or k
+__device__ __forceinline__ uint32_t find_start(const unsigned long long* r, uint32_t k, uint64_t pos) {
+  uint32_t lo = 0, hi = k;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) / 2;
+    if (r[mid] < pos) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo < k && r[lo] == pos ? lo : k;
+}
+
+template <typename S, int D>
+__global__ void parse_stitch(const __grid_constant__ Job job, uint64_t seg, uint32_t k, uint32_t workers,
+                             const unsigned long long* rec) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const BlockParams p{job.minbits, job.maxbits, job.maxprec, job.minexp};
+  uint64_t pos = job.bit0, b = 0;
+  uint32_t miss = 0;   // blocks parsed here since the last search
+  while (b < job.nblocks) {
+    if (miss == 0 || miss >= 8) {
+      // workers that started at or before pos, latest first
+      const uint64_t w_hi = (pos - job.bit0) / seg;
+      bool adopted = false;
+      for (uint64_t d = 0; d <= 4 && d <= w_hi && !adopted; d++) {
+        const uint64_t w = w_hi - d;
+        if (w >= workers) continue;
+        const unsigned long long* r = rec + (size_t)w * (k + 1);
+        if (r[k] <= pos) break;   // this and earlier workers end before pos
+        const uint32_t j = find_start(r, k, pos);
+        if (j == k) continue;
+        uint32_t i = j;
+        for (; i < k && b < job.nblocks; i++) job.offsets[b++] = r[i];
+        pos = r[i];   // start of the next block: the end of the last one taken
+        adopted = true;
+      }
+      miss = adopted ? 0 : 1;
+      if (adopted) continue;
+    }
+    WordSource in;
+    in.base = job.words;
+    in.cap = job.cap_words;
+    in.seek(pos);
+    job.offsets[b++] = pos;
+    skip_block<S, D>(in, p);
+    pos = in.tell();
+    miss++;
+  }
+  job.result->end_bit = pos;
+}
+
 }  // namespace zg

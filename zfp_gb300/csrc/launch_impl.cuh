@@ -135,10 +135,48 @@ cudaError_t run_decode(const LaunchArgs& a, cudaStream_t st) {
   });
 }
 
+// Block offsets of a stream with no index (kernels.cuh: parse_kernel, and
+// the speculative parse_probe / parse_spec / parse_stitch for long streams).
+// Synchronous: returns after the offsets and end bit are written.
 template <typename S, int D>
 cudaError_t run_parse(const Job& job, cudaStream_t st) {
-  parse_kernel<S, D><<<1, 32, 0, st>>>(job);
-  return cudaGetLastError();
+  constexpr uint32_t kProbe = 256;
+  const uint64_t seg_blocks = std::max<uint64_t>(2048, job.nblocks / 2048);
+  const uint32_t k = (uint32_t)(4 * seg_blocks);   // blocks each worker records
+  if (job.nblocks <= 4ull * k) {
+    parse_kernel<S, D><<<1, 32, 0, st>>>(job);
+    cudaError_t e = cudaGetLastError();
+    return e != cudaSuccess ? e : cudaStreamSynchronize(st);
+  }
+  unsigned long long* mean = nullptr;
+  unsigned long long* rec = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&mean, sizeof *mean, st);
+  if (e != cudaSuccess) return e;
+  unsigned long long mean_bits = 0;
+  parse_probe<S, D><<<1, 32, 0, st>>>(job, kProbe, mean);
+  if ((e = cudaGetLastError()) != cudaSuccess ||
+      (e = cudaMemcpyAsync(&mean_bits, mean, sizeof mean_bits, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+    cudaFreeAsync(mean, st);
+    return e;
+  }
+  const uint64_t seg = std::max<uint64_t>(mean_bits, 1) * seg_blocks;   // bits between worker starts
+  // cover the stream's estimated length and a quarter more, within 512 MB of
+  // records; beyond, the stitch parses alone
+  const uint64_t want = std::max<uint64_t>(mean_bits, 1) * job.nblocks * 5 / 4 / seg + 4;
+  const uint64_t room = (512ull << 20) / (8ull * (k + 1));
+  const uint32_t workers = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(want, room), 8192);
+  e = cudaMallocAsync((void**)&rec, (size_t)workers * (k + 1) * sizeof *rec, st);
+  if (e == cudaSuccess) {
+    parse_spec<S, D><<<(workers + 127) / 128, 128, 0, st>>>(job, seg, k, workers, rec);
+    if ((e = cudaGetLastError()) == cudaSuccess) {
+      parse_stitch<S, D><<<1, 32, 0, st>>>(job, seg, k, workers, rec);
+      e = cudaGetLastError();
+    }
+    cudaFreeAsync(rec, st);
+  }
+  cudaFreeAsync(mean, st);
+  return e != cudaSuccess ? e : cudaStreamSynchronize(st);
 }
 
 }  // namespace zg
