@@ -667,6 +667,10 @@ __global__ void parse_kernel(const __grid_constant__ Job job) {
 // Every adopted offset therefore follows from a position reached by the
 // true chain: the result is the sequential parse's, only faster.
 
+// a worker records the chain over this many worker spacings, so up to this
+// many workers cover any position
+constexpr uint32_t kParseCover = 16;
+
 template <typename S, int D>
 __global__ void parse_probe(const __grid_constant__ Job job, uint32_t count, unsigned long long* mean_bits) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -714,13 +718,13 @@ __global__ void parse_stitch(const __grid_constant__ Job job, uint64_t seg, uint
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const BlockParams p{job.minbits, job.maxbits, job.maxprec, job.minexp};
   uint64_t pos = job.bit0, b = 0;
-  uint32_t miss = 0;   // blocks parsed here since the last search
+  uint32_t miss = 0, wait = 0;   // blocks parsed here since the last search; before the next
   while (b < job.nblocks) {
-    if (miss == 0 || miss >= 8) {
+    if (miss >= wait) {
       // workers that started at or before pos, latest first
       const uint64_t w_hi = (pos - job.bit0) / seg;
       bool adopted = false;
-      for (uint64_t d = 0; d <= 4 && d <= w_hi && !adopted; d++) {
+      for (uint64_t d = 0; d < kParseCover && d <= w_hi && !adopted; d++) {
         const uint64_t w = w_hi - d;
         if (w >= workers) continue;
         const unsigned long long* r = rec + (size_t)w * (k + 1);
@@ -732,8 +736,12 @@ __global__ void parse_stitch(const __grid_constant__ Job job, uint64_t seg, uint
         pos = r[i];   // start of the next block: the end of the last one taken
         adopted = true;
       }
-      miss = adopted ? 0 : 1;
-      if (adopted) continue;
+      miss = 0;
+      if (adopted) {
+        wait = 0;
+        continue;
+      }
+      wait = wait ? (wait < 64 ? 2 * wait : 64) : 8;   // searching again soon rarely pays
     }
     WordSource in;
     in.base = job.words;

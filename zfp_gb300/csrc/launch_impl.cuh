@@ -141,8 +141,8 @@ cudaError_t run_decode(const LaunchArgs& a, cudaStream_t st) {
 template <typename S, int D>
 cudaError_t run_parse(const Job& job, cudaStream_t st) {
   constexpr uint32_t kProbe = 256;
-  const uint64_t seg_blocks = std::max<uint64_t>(2048, job.nblocks / 2048);
-  const uint32_t k = (uint32_t)(4 * seg_blocks);   // blocks each worker records
+  const uint64_t seg_blocks = std::max<uint64_t>(512, job.nblocks / 4096);
+  const uint32_t k = (uint32_t)(kParseCover * seg_blocks);   // blocks each worker records
   if (job.nblocks <= 4ull * k) {
     parse_kernel<S, D><<<1, 32, 0, st>>>(job);
     cudaError_t e = cudaGetLastError();
