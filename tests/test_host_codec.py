@@ -198,3 +198,36 @@ def test_length_only_parse_matches_oracle_block_ends(host, oracle, dims, dtype):
         got = host.zgh_parse(ZTYPE[np.dtype(dtype)], dims, n, p, C.c_void_p(words.ctypes.data),
                              C.c_uint64(len(words)), C.c_uint64(bit0), C.c_void_p(ends.ctypes.data))
         assert got == end and np.array_equal(ends, be), (mode, arg, shape)
+
+
+@pytest.mark.parametrize("dims", [1, 2, 3])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64, np.int32, np.int64], ids=lambda d: np.dtype(d).name)
+def test_decoder_on_random_words_matches_oracle(host, oracle, dims, dtype):
+    """Any bit string is a stream: decoding random words drives the plane
+    decoder (windowed group tests, budget and last-coefficient limits)
+    through code patterns an encoder rarely writes."""
+    rng = np.random.default_rng(300 + dims * 7 + ZTYPE[np.dtype(dtype)])
+    modes = [("rate", 4), ("rate", 12.5), ("rate", 40), ("precision", 20), ("precision", 64),
+             ("reversible", None), ("expert", (30, 70, 33, -5)), ("expert", (0, 4000, 64, -1074))]
+    for mode, arg in modes:
+        for density in (0.5, 0.9, 0.1):
+            shape = tuple(int(v) for v in rng.integers(1, {1: 60, 2: 17, 3: 9}[dims], size=dims))
+            prm = mode_params(mode, arg, dtype, dims)
+            nw = oracle.max_words(tuple(reversed(shape)), np.dtype(dtype), prm) + 8
+            words = np.zeros(nw, dtype=np.uint64)
+            for b in range(64):
+                words |= (rng.random(nw) < density).astype(np.uint64) << np.uint64(b)
+            d0 = np.zeros(shape, dtype=dtype)
+            d1 = np.zeros(shape, dtype=dtype)
+            x0 = oracle.decompress(words, d0, prm, 0)
+            x1 = host_decompress(host, words.copy(), d1, prm, 0)
+            assert x0 == x1 and np.array_equal(d0.view(np.uint8), d1.view(np.uint8)), (mode, arg, shape, density)
+            # the length-only parse ends where the decoder ended
+            n = (C.c_size_t * 4)(*(list(reversed(shape)) + [0] * (4 - dims)))
+            p = (C.c_uint * 4)(*[v & 0xffffffff for v in prm])
+            nb = int(np.prod([(v + 3) // 4 for v in shape]))
+            ends = np.zeros(nb, dtype=np.uint64)
+            host.zgh_parse.restype = C.c_uint64
+            got = host.zgh_parse(ZTYPE[np.dtype(dtype)], dims, n, p, C.c_void_p(words.ctypes.data),
+                                 C.c_uint64(len(words)), C.c_uint64(0), C.c_void_p(ends.ctypes.data))
+            assert got == x0, (mode, arg, shape, density)

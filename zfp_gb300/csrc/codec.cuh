@@ -118,6 +118,40 @@ ZG_HD int clz64(uint64_t x) {
 #endif
 }
 
+ZG_HD unsigned ctz32(uint32_t x) {      // x nonzero
+#if defined(__CUDA_ARCH__)
+  return (unsigned)__clz(__brev(x));
+#else
+  return (unsigned)__builtin_ctz(x);
+#endif
+}
+
+ZG_HD unsigned clz32(uint32_t x) {      // x nonzero
+#if defined(__CUDA_ARCH__)
+  return (unsigned)__clz(x);
+#else
+  return (unsigned)__builtin_clz(x);
+#endif
+}
+
+ZG_HD unsigned popc32(uint32_t x) {
+#if defined(__CUDA_ARCH__)
+  return (unsigned)__popc(x);
+#else
+  return (unsigned)__builtin_popcount(x);
+#endif
+}
+
+// bit j of the result: parity of bits 0..j of x
+ZG_HD uint32_t prefix_xor32(uint32_t x) {
+  x ^= x << 1;
+  x ^= x << 2;
+  x ^= x << 4;
+  x ^= x << 8;
+  x ^= x << 16;
+  return x;
+}
+
 // ---------------------------------------------------------------------------
 // coefficient order (src/template/codec{2,3,4}.c): by total sequency
 // i+j+k(+l), then by i^2+j^2+k^2(+l^2); ties in the order the format fixes.
@@ -737,15 +771,49 @@ ZG_HD unsigned encode_planes(Sink& out, unsigned budget, unsigned maxprec, const
 // positive group test and the scan that follows it are read with one peek.
 // When the budget ends inside a positive group test the reference still
 // deposits a one at the scan position; so does this.
+// Whole events of a 32-bit window of group-test code that starts at a
+// positive test.  Past a plane's verbatim bits its code is a run of events
+// "1 0^z 1" (positive test, z zero scan bits, the one found) ended by a 0
+// (src/template/decode.c:100-113).  The prefix parity of the window is 1
+// exactly inside an event (from its test up to its found one), so a 0 of
+// parity 0 ends the plane and the ones of parity 0 are the found ones.
+// e: bits of the whole events (up to the stop, else up to the last found
+// one; 0 if the window holds none); scan: scan bits among them (each stands
+// for the next coefficient, n, n+1, ...; so after them n grows by scan);
+// found: their found ones; used: bits to consume (the stop included).
+struct EventWindow {
+  uint32_t found;
+  unsigned e, scan, used;
+  bool stop;
+};
+
+ZG_HD EventWindow event_window(uint32_t w) {
+  const uint32_t px = prefix_xor32(w);
+  const uint32_t stop = ~(w | px);
+  const uint32_t found = w & ~px;
+  EventWindow ev;
+  ev.e = stop ? ctz32(stop) : found ? 32 - clz32(found) : 0;
+  const uint32_t seg = ev.e >= 32 ? ~0u : (1u << ev.e) - 1;
+  ev.scan = ev.e - popc32(w & px & seg);
+  ev.found = found & seg;
+  ev.stop = stop != 0;
+  ev.used = ev.e + (stop != 0);
+  return ev;
+}
+
 struct PlaneBuf {
   uint64_t* p;
   int stride;
 };
 
+// kWin: decode group tests a 32-bit window at a time (event_window) where
+// the window holds whole events; measured faster for lossy blocks, which
+// have several events per plane, and slower for reversible ones, which have
+// about one per plane before every coefficient is significant.
 // Planes below the last one decoded are zero.  For 64-bit coefficients,
 // when every decoded plane lies in the top half, only the top half is
 // stored (zeros included) and `top_only` is set: the low words are zero.
-template <int P, int N, class Source>
+template <int P, int N, class Source, bool kWin = true>
 ZG_HD unsigned decode_planes(Source& in, unsigned budget, unsigned maxprec, PlaneBuf pb, bool& top_only) {
   const int kmin = (unsigned)P > maxprec ? P - (int)maxprec : 0;
   unsigned bits = budget, n = 0;
@@ -755,6 +823,46 @@ ZG_HD unsigned decode_planes(Source& in, unsigned budget, unsigned maxprec, Plan
     uint64_t x = in.read(m);
     bits -= m;
     while (bits && n < (unsigned)N) {
+      if (kWin && bits >= 32 && n + 1 < (unsigned)N) {
+        const uint32_t w = in.peek32();
+        if (!(w & 1)) {        // negative test: rest of the plane is zero
+          in.skip(1);
+          bits--;
+          break;
+        }
+        if (w != 1) {          // else no found one in the window
+          const EventWindow ev = event_window(w);
+          // found one of rank i (from 1) at window bit j: coefficient
+          // n + j - i.  Events are taken while their found one lies below
+          // the last coefficient (which is implied, never scanned).
+          const int room = N - 2 - (int)n;
+          uint32_t f = ev.found, y = 0;
+          int i = 1, last = -1;
+          for (; f; i++) {
+            const int j = (int)ctz32(f);
+            if (j - i > room) break;
+            y |= 1u << (j - i);
+            last = j;
+            f &= f - 1;
+          }
+          x |= (uint64_t)y << n;
+          if (!f) {            // every event of the window
+            n += ev.scan;
+            in.skip(ev.used);
+            bits -= ev.used;
+            if (ev.stop) break;
+            continue;
+          }
+          if (last >= 0) {     // the events before one that reaches the limit
+            n += (unsigned)(last + 2 - i);
+            in.skip((unsigned)last + 1);
+            bits -= (unsigned)last + 1;
+            continue;
+          }
+        }
+      }
+      // one event at a time: near the budget or the last coefficient, or a
+      // scan longer than the window
       const uint64_t w = in.peek64();
       if (!(w & 1)) {          // negative test: rest of the plane is zero
         in.skip(1);
@@ -848,7 +956,7 @@ ZG_HD unsigned decode_planes_wide(Source& in, unsigned budget, unsigned maxprec,
 // integer block codec (src/template/encode.c:260-280, decode.c:282-298,
 // revencode.c:57-79, revdecode.c:37-55)
 
-template <int D, typename I, class Source>
+template <int D, typename I, class Source, bool kWin = true>
 ZG_HD unsigned uncode_coeffs(Source& in, unsigned budget, unsigned maxprec,
                              typename std::make_unsigned<I>::type (&u)[1 << (2 * D)], PlaneBuf pb) {
   using U = typename std::make_unsigned<I>::type;
@@ -856,7 +964,7 @@ ZG_HD unsigned uncode_coeffs(Source& in, unsigned budget, unsigned maxprec,
   constexpr int P = 8 * sizeof(U);
   if constexpr (N <= 64) {
     bool top_only;
-    const unsigned bits = decode_planes<P, N>(in, budget, maxprec, pb, top_only);
+    const unsigned bits = decode_planes<P, N, Source, kWin>(in, budget, maxprec, pb, top_only);
     if constexpr (P == 64 && N > 4) {
       if (top_only) {
         uint64_t pl[32];
@@ -900,7 +1008,7 @@ ZG_HD unsigned rev_decode_ints(Source& in, unsigned minbits, unsigned maxbits, I
   constexpr unsigned kPBits = sizeof(I) == 4 ? 5 : 6;
   const unsigned prec = (unsigned)in.read(kPBits) + 1;
   U u[N];
-  unsigned bits = kPBits + uncode_coeffs<D, I>(in, maxbits - kPBits, prec, u, pb);
+  unsigned bits = kPBits + uncode_coeffs<D, I, Source, false>(in, maxbits - kPBits, prec, u, pb);
   if (bits < minbits) { in.skip_long(minbits - bits); bits = minbits; }
 #pragma unroll (N <= 64 ? N : 1)
   for (int i = 0; i < N; i++) v[perm<D>(i)] = from_nb<I>(u[i]);
@@ -1377,6 +1485,19 @@ ZG_HD unsigned skip_planes(Source& in, unsigned budget, unsigned maxprec) {
       m -= c;
     }
     while (bits && n < (unsigned)N) {
+      if (bits >= 32 && n + 1 < (unsigned)N) {
+        const uint32_t w = in.peek32();
+        if ((w & 1) && w != 1) {
+          const EventWindow ev = event_window(w);
+          if (ev.e && n + ev.scan < (unsigned)N) {
+            n += ev.scan;
+            in.skip(ev.used);
+            bits -= ev.used;
+            if (ev.stop) break;
+            continue;
+          }
+        }
+      }
       const bool positive = in.peek64() & 1;
       in.skip(1);
       bits--;
@@ -1502,6 +1623,16 @@ struct WordSourceT {
     pos = (unsigned)(bit & 63);
   }
   ZG_HD uint64_t peek64() const { return pos ? (lo >> pos) | (hi << (64 - pos)) : lo; }
+  ZG_HD uint32_t peek32() const {
+#if defined(__CUDA_ARCH__)
+    const bool up = pos >= 32;
+    const uint32_t a = up ? (uint32_t)(lo >> 32) : (uint32_t)lo;
+    const uint32_t b = up ? (uint32_t)hi : (uint32_t)(lo >> 32);
+    return __funnelshift_r(a, b, pos);
+#else
+    return (uint32_t)peek64();
+#endif
+  }
   ZG_HD uint64_t peek(unsigned n) const { return low_bits(peek64(), n); }   // n <= 64
   ZG_HD void skip(unsigned n) {               // n <= 64
     pos += n;
