@@ -301,16 +301,19 @@ __device__ __forceinline__ void publish_state(unsigned long long* slot, unsigned
   *(volatile unsigned long long*)slot = v;
 }
 
-// Called by all lanes of warp 0.  Returns the number of stream bits taken by
-// the job's tiles before `gt`.
+// The tile's own bit total, published by one thread as soon as it is known
+// (the job's first tile publishes it as its inclusive prefix).
+__device__ __forceinline__ void publish_aggregate(const Job& job, const LaunchScratch& sc, uint32_t gt,
+                                                  uint64_t aggregate) {
+  publish_state(sc.tile_state + gt, (gt == job.tile0 ? kStateIncl : kStateAgg) | aggregate);
+}
+
+// Called by all lanes of one warp after publish_aggregate.  Returns the
+// number of stream bits taken by the job's tiles before `gt`.
 __device__ __forceinline__ uint64_t look_back(const Job& job, const LaunchScratch& sc, uint32_t gt,
                                               uint64_t aggregate) {
   const unsigned lane = threadIdx.x & 31;
-  if (gt == job.tile0) {
-    if (lane == 0) publish_state(sc.tile_state + gt, kStateIncl | aggregate);
-    return 0;
-  }
-  if (lane == 0) publish_state(sc.tile_state + gt, kStateAgg | aggregate);
+  if (gt == job.tile0) return 0;
   uint64_t exclusive = 0;
   int64_t pred = (int64_t)gt - 1 - lane;
   const long long t0 = clock64();
@@ -444,13 +447,12 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
   uint64_t* img = in_smem ? simg : gslot;
   const uint32_t nw = min(need, img_cap(in_smem ? img_words : slot_words));
   for (uint32_t i = threadIdx.x; i < nw; i += kTile) img[img_phys(i)] = 0;
-  if (fixed && threadIdx.x == 0) s_base = (unsigned long long)lt * kTile * job.maxbits;
+  if (threadIdx.x == 0) {
+    if (fixed) s_base = (unsigned long long)lt * kTile * job.maxbits;
+    else publish_aggregate(job, sc, gt, total);
+  }
   __syncthreads();
 
-  if (!fixed && threadIdx.x < 32) {
-    const uint64_t before = look_back(job, sc, gt, total);
-    if (threadIdx.x == 0) s_base = before;
-  }
   if (active) {
     if constexpr (N <= 64) {
       SmemSink seq{img, excl >> 6, excl & 63u, 0ull, true, nw, &job.result->status};
@@ -461,6 +463,13 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
       wc.emit(out);
       out.finish();
     }
+  }
+  // the tile's place in the stream is needed only by write_tile: the last
+  // warp resolves it after its own blocks, by when the predecessors have
+  // mostly published theirs
+  if (!fixed && threadIdx.x >= kTile - 32) {
+    const uint64_t before = look_back(job, sc, gt, total);
+    if (threadIdx.x == kTile - 32) s_base = before;
   }
   __syncthreads();
 
@@ -474,6 +483,28 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
 template <typename S, int D, bool kEncode>
 constexpr size_t plane_smem_bytes() {
   return (1 << (2 * D)) <= 64 ? (size_t)8 * sizeof(typename Traits<S>::UInt) * kTile * 8 : 0;
+}
+
+// 64-bit 2D/3D blocks whose coded planes all lie in the top half (maxprec <=
+// 32: every lossy mode but high precision) never touch planes 0-31 -- the
+// encoder transposes only the high words and the decoder keeps `top_only`
+// -- so a single-job launch gives them only the upper half of the plane
+// buffer.  Host and kernel decide it from the same job.
+template <typename S, int D>
+ZG_HD constexpr bool half_planes(unsigned maxprec) {
+  return sizeof(typename Traits<S>::UInt) == 8 && D >= 2 && D <= 3 && maxprec <= 32;
+}
+
+template <typename S, int D, bool kEncode>
+ZG_HD constexpr size_t plane_smem_bytes(bool multi, unsigned maxprec) {
+  return !multi && half_planes<S, D>(maxprec) ? plane_smem_bytes<S, D, kEncode>() / 2 : plane_smem_bytes<S, D, kEncode>();
+}
+
+// plane k of thread 0 at planes[k * kTile]: the buffer starts at plane 32
+// when it holds only the upper half
+template <typename S, int D, bool kMulti>
+__device__ __forceinline__ uint64_t* plane_base(uint64_t* buf, const Job& one) {
+  return !kMulti && half_planes<S, D>(one.maxprec) ? buf - 32 * kTile : buf;
 }
 
 // ---------------------------------------------------------------------------
@@ -510,6 +541,11 @@ __device__ __forceinline__ void decode_tile(const Job& job, uint32_t gt, uint64_
   if (staged) {
     for (uint64_t i = threadIdx.x; i < nwords; i += kTile)
       img[img_phys((uint32_t)i)] = w0 + i < job.cap_words ? __ldg((const unsigned long long*)job.words + w0 + i) : 0ull;
+  } else {
+    // each thread walks its block's words one dependent load at a time:
+    // bring the tile's lines into L2 first (16 words a line)
+    for (uint64_t i = 16 * threadIdx.x; i < nwords && w0 + i < job.cap_words; i += 16 * kTile)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(job.words + w0 + i)));
   }
   __syncthreads();
   if (!active) return;
@@ -564,7 +600,7 @@ __device__ __forceinline__ void encode_body(const Job& one, const Job* jobs, int
                                             uint32_t slot_words, uint32_t img_words) {
   extern __shared__ uint64_t smem_img[];
   uint64_t* gslot = gimg ? gimg + (size_t)blockIdx.x * slot_words : nullptr;
-  uint64_t* planes = smem_img + img_words;
+  uint64_t* planes = plane_base<S, D, kMulti>(smem_img + img_words, one);
   __shared__ uint32_t s_tile;
   __shared__ Job s_job;
   for (uint32_t iter = blockIdx.x;; iter += gridDim.x) {
@@ -601,7 +637,7 @@ __device__ __forceinline__ void decode_body(const Job& one, const Job* jobs, int
                                             uint32_t img_words) {
   extern __shared__ uint64_t smem_img[];
   uint64_t* img = smem_img;
-  uint64_t* planes = smem_img + img_words;
+  uint64_t* planes = plane_base<S, D, kMulti>(smem_img + img_words, one);
   __shared__ Job s_job;
   for (uint32_t gt = blockIdx.x; gt < total_tiles; gt += gridDim.x) {
     const Job* job = resolve_job<kMulti>(one, jobs, njobs, gt, &s_job);

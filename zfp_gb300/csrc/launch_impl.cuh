@@ -83,6 +83,7 @@ static auto with_encoder(const LaunchArgs& a, F&& f) {
   }
   if constexpr (sizeof(S) == 4 && D <= 3) {
     if (five_ctas<S, D>(a.one)) return f(KernelTag<encode_kernel_occ<S, D, false, kLossyOnly, 5>>{});
+    if constexpr (D == 3) return f(KernelTag<encode_kernel_occ<S, D, false, kLossyOnly, 4>>{});
   }
   return f(KernelTag<encode_kernel<S, D, false, kLossyOnly>>{});
 }
@@ -98,13 +99,16 @@ static auto with_decoder(const LaunchArgs& a, F&& f) {
     return f(KernelTag<decode_kernel_occ<S, D, false, kLossyOnly, 3>>{});
   } else {
     if (five_ctas<S, D>(a.one)) return f(KernelTag<decode_kernel_occ<S, D, false, kLossyOnly, 5>>{});
-    return f(KernelTag<decode_kernel<S, D, false, kLossyOnly>>{});
+    if constexpr (sizeof(S) == 4 && D == 3) return f(KernelTag<decode_kernel_occ<S, D, false, kLossyOnly, 4>>{});
+    else return f(KernelTag<decode_kernel<S, D, false, kLossyOnly>>{});
   }
 }
 
 template <typename S, int D>
 uint32_t stage_room(const LaunchArgs& a, bool encode) {
-  const size_t planes = encode ? plane_smem_bytes<S, D, true>() : plane_smem_bytes<S, D, false>();
+  const bool multi = a.jobs != nullptr;
+  const size_t planes = encode ? plane_smem_bytes<S, D, true>(multi, a.one.maxprec)
+                               : plane_smem_bytes<S, D, false>(multi, a.one.maxprec);
   auto words = [&](auto tag) -> uint32_t {
     const size_t r = smem_room<decltype(tag)::kernel>();
     return r > planes ? (uint32_t)((r - planes) / 8) : 0u;
@@ -114,7 +118,7 @@ uint32_t stage_room(const LaunchArgs& a, bool encode) {
 
 template <typename S, int D>
 cudaError_t run_encode(const LaunchArgs& a, cudaStream_t st) {
-  const size_t smem = (size_t)a.img_words * 8 + plane_smem_bytes<S, D, true>();
+  const size_t smem = (size_t)a.img_words * 8 + plane_smem_bytes<S, D, true>(a.jobs != nullptr, a.one.maxprec);
   return with_encoder<S, D>(a, [&](auto tag) {
     constexpr auto kernel = decltype(tag)::kernel;
     prepare_kernel<kernel>();
@@ -126,7 +130,7 @@ cudaError_t run_encode(const LaunchArgs& a, cudaStream_t st) {
 
 template <typename S, int D>
 cudaError_t run_decode(const LaunchArgs& a, cudaStream_t st) {
-  const size_t smem = (size_t)a.img_words * 8 + plane_smem_bytes<S, D, false>();
+  const size_t smem = (size_t)a.img_words * 8 + plane_smem_bytes<S, D, false>(a.jobs != nullptr, a.one.maxprec);
   return with_decoder<S, D>(a, [&](auto tag) {
     constexpr auto kernel = decltype(tag)::kernel;
     prepare_kernel<kernel>();
