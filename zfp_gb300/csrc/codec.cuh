@@ -1340,16 +1340,16 @@ ZG_HD unsigned emit_block(Sink& out, const BlockHead& h, const uint64_t* plane, 
 //    and, if anything above n is set, the opening positive group test; the
 //    rest of the plane's code is skipped (pad) and filled in by pass 2.
 //    Planes with such bits ("event planes") are remembered: the slot of
-//    plane k is overwritten with r = x >> n;
+//    plane k is overwritten with r = x >> n, a flag for an implied last one
+//    and the block-relative bit b = start + n + 1 (r << 16 | flag << 15 | b;
+//    the one plane a block may have with r >= 2^48 keeps flag and b in a
+//    register);
 //  pass 2, one flat loop over every one bit of every event plane, through
-//    the positional sink `pos` (out.set(at, v, n): OR v, n bits, at the
-//    block-relative bit `at`).  n changes only at event planes, so the
-//    planes between two event planes each take n + 1 bits (n once all
-//    coefficients are significant) and an event plane's start and length
-//    follow from r alone: pass 2 walks the event planes with no stored
-//    offsets.  The j-th one at offset p of r sits at start + n + 1 + p + j
-//    and, unless it is the plane's last one, is followed by a positive test;
-//    a last one at the last coefficient is implied and not written.
+//    the positional sink `pos` (out.set_small(at, v, n): OR v, n bits, at
+//    the block-relative bit `at`).  The j-th one at offset p of r sits at
+//    b + p + j and, unless it is the plane's last one, is followed by a
+//    positive test; a last one at the last coefficient is implied and not
+//    written.  A new event plane costs pass 2 one shared-memory load.
 // Zeros need no writes, and bits at or past the budget are dropped, which
 // cuts the code exactly where the reference's bit budget stops the coder
 // (src/template/encode.c:92-256).  Pass 2 runs once per event of the block
@@ -1361,6 +1361,8 @@ ZG_HD unsigned emit_block_2p(Seq& seq, Pos& pos, const BlockHead& h, uint64_t* p
   seq.put(h.hdr, h.hdr_bits);
   unsigned bits = h.hdr_bits;
   Mask events = 0;                        // bit k: plane k has ones above its n
+  int wide_k = -1;                        // the event plane whose r needs all 64 bits, if any
+  unsigned wide_meta = 0;
   // positions fit 16 bits: a block's code is at most P * (N + 2) + N bits
   unsigned lim = 0;
   if (h.coded) {
@@ -1379,7 +1381,20 @@ ZG_HD unsigned emit_block_2p(Seq& seq, Pos& pos, const BlockHead& h, uint64_t* p
       const unsigned ev = n != n0 && room > m;               // opening positive test of an event plane
       seq.put(low_bits(x, m) | ((uint64_t)ev << m), m + ev);
       if (ev) {
-        plane[k * stride] = x >> n0;
+        // pass 2 finds the plane's ones, whether the last one is implied
+        // and where the first one's position is counted from (a block's
+        // code is under 2^15 bits) in the plane's slot: r << 16 | meta.
+        // At most one plane has r >= 2^48 (it needs n < 16 before and
+        // leaves n > 48): its slot holds r, its meta a register.
+        const uint64_t r = x >> n0;
+        const unsigned meta = ((unsigned)(n >= (unsigned)N) << 15) | (at + n0 + 1);
+        if (!(r >> 48)) {
+          plane[k * stride] = (r << 16) | meta;
+        } else {
+          plane[k * stride] = r;
+          wide_k = k;
+          wide_meta = meta;
+        }
         events |= Mask(1) << k;
       }
       seq.pad(room - m - ev);
@@ -1399,21 +1414,18 @@ ZG_HD unsigned emit_block_2p(Seq& seq, Pos& pos, const BlockHead& h, uint64_t* p
   }
   seq.finish();
   uint64_t r = 0;
-  unsigned at = h.hdr_bits, n = 0, b = 0;   // at: start of the plane below the last event plane
-  int kprev = P;
+  unsigned b = 0;                           // the j-th one at offset p of r sits at b + p + j
   bool implied = false;
   while (r || events) {
     if (!r) {
       const int k = 63 - clz64((uint64_t)events);
       events &= ~(Mask(1) << k);
-      at += (unsigned)(kprev - 1 - k) * (n < (unsigned)N ? n + 1 : n);   // planes without events
-      kprev = k;
-      r = plane[k * stride];
-      const unsigned top = n + 64 - (unsigned)clz64(r);              // n after this plane
-      b = at + n + 1;                                                // the j-th one at offset p sits at b + p + j
-      implied = top >= (unsigned)N;
-      at += top + (unsigned)popc64(r) + (implied ? 0u : 1u) - (implied ? 1u : 0u);
-      n = top;
+      const uint64_t v = plane[k * stride];
+      const bool wide = k == wide_k;
+      r = wide ? v : v >> 16;
+      const unsigned meta = wide ? wide_meta : (unsigned)v;
+      implied = (meta >> 15) & 1;
+      b = meta & 0x7fffu;
     }
     const unsigned p = b + ctz64(r);
     r &= r - 1;
