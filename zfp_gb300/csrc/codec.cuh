@@ -1400,7 +1400,14 @@ ZG_HD unsigned emit_block_2p(Seq& seq, Pos& pos, const BlockHead& h, uint64_t* p
       seq.pad(room - m - ev);
       at += len;
     }
-    // once every coefficient is significant a plane is its N bits, verbatim
+    // once every coefficient is significant a plane is its N bits, verbatim:
+    // whole 64-bit planes first (a constant-width put), then one cut plane
+    if constexpr (N == 64) {
+      for (; k >= kmin && at + 64u <= lim; k--) {
+        seq.put(plane[k * stride], 64);
+        at += 64;
+      }
+    }
     for (; k >= kmin && at < lim; k--) {
       const unsigned m = lim - at < (unsigned)N ? lim - at : (unsigned)N;
       seq.put(low_bits(plane[k * stride], m), m);
