@@ -703,8 +703,9 @@ def e2e_run(lib, torch, codec, fields, args):
     _, world, _ = dist_info()
     return {"value": round(world * raw_step * n / dt / 1e9, 2), "unit": "GB/s", "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "steps": n,
-            "buffers": "pinned host field and stream, read and written in place by the kernels over the host link "
-                       "(h2d/d2h = bytes crossing it)", "staged_bytes_per_step": staged[0]}
+            "buffers": "pinned host field and stream, read and written in place by the kernels over the host link, "
+                       "except streams whose decode tiles outgrow shared memory, uploaded once (staged_bytes_per_step); "
+                       "h2d/d2h = bytes crossing the link", "staged_bytes_per_step": staged[0]}
 
 
 # ---------------------------------------------------------------------------

@@ -273,7 +273,9 @@ def test_pinned_host_buffers_zero_copy(lib, oracle, cuda):
     as the oracle; pageable host buffers are still staged."""
     torch = cuda
     tdt = {np.float32: torch.float32, np.float64: torch.float64, np.int32: torch.int32, np.int64: torch.int64}
-    cases = [(np.float32, (37, 45, 66), "rate", 8), (np.float64, (21, 30, 47), "accuracy", 1e-4),
+    # (64-bit accuracy tiles can outgrow the decoder's shared memory, and
+    # such streams are uploaded instead: see the test below)
+    cases = [(np.float32, (37, 45, 66), "rate", 8), (np.float64, (21, 30, 47), "precision", 24),
              (np.int32, (300, 301), "precision", 20), (np.float32, (40, 64, 90), "reversible", None),
              (np.int64, (9, 10, 11, 12), "rate", 12)]
     for dtype, shape, mode, arg in cases:
@@ -304,6 +306,31 @@ def test_pinned_host_buffers_zero_copy(lib, oracle, cuda):
         r3, _ = zfp_run(lib, "decompress", out2.ctypes.data, zt, n, s, mode, arg, page.ctypes.data, nwords * 8)
         assert r3 == r and lib.zfp_gb300_last_staged_bytes() > 0, msg
         assert np.array_equal(out2.view(np.uint8), ref_out.view(np.uint8)), msg
+
+
+def test_pinned_stream_uploaded_when_tiles_exceed_shared_memory(lib, oracle, cuda):
+    """A page-locked stream whose decode tiles do not fit the decoder's shared
+    memory (64-bit reversible: about 60 KB a tile) is uploaded once instead
+    of being read word by word across the host link; 32-byte row stores
+    write the 64-bit field.  Same bits as the oracle either way."""
+    torch = cuda
+    shape = (24, 40, 64)
+    vals = np.random.default_rng(5).standard_normal(shape) * 1e3   # about 64 bits a value
+    exp_words, _, prm = oracle_stream(oracle, vals, "reversible", None)
+    nwords = len(exp_words) + 16
+    hx = torch.empty(shape, dtype=torch.float64, pin_memory=True)
+    hx.numpy()[...] = vals
+    hs = torch.zeros(nwords, dtype=torch.int64, pin_memory=True)
+    n, s = geometry(vals)
+    zt = ztype_of(vals)
+    r, _ = zfp_run(lib, "compress", hx.data_ptr(), zt, n, s, "reversible", None, hs.data_ptr(), nwords * 8)
+    assert r == len(exp_words) * 8, lib.zfp_gb300_last_error()
+    assert lib.zfp_gb300_last_staged_bytes() == 0
+    assert np.array_equal(hs.numpy().view(np.uint64)[: len(exp_words)], exp_words)
+    hout = torch.zeros(shape, dtype=torch.float64, pin_memory=True)
+    r2, _ = zfp_run(lib, "decompress", hout.data_ptr(), zt, n, s, "reversible", None, hs.data_ptr(), nwords * 8)
+    assert r2 == r and lib.zfp_gb300_last_staged_bytes() == r
+    assert np.array_equal(hout.numpy().view(np.uint64), vals.view(np.uint64))
 
 
 def test_foreign_stream_long_parallel_parse(lib, cuda):

@@ -153,7 +153,7 @@ zfp_gb300_batch* zfp_gb300_batch_create(zfp_stream* const* streams, const zfp_fi
     }
     const bool fixed = is_fixed_rate(fi, z);
     Job j = base_job(fi, z, f->data);
-    j.flags = (fixed ? kFixedRate : 0u) | (vector_ok(fi, f->data) ? kVecOk : 0u);
+    j.flags = (fixed ? kFixedRate : 0u) | vector_flags(fi, f->data);
     j.words = ss.begin;
     j.cap_words = (uint64_t)(ss.end - ss.begin);
     j.result = b->d_results + i;

@@ -210,6 +210,14 @@ bool vector_ok(const FieldInfo& fi, const void* data) {
   return true;
 }
 
+uint32_t vector_flags(const FieldInfo& fi, const void* data) {
+  if (!vector_ok(fi, data)) return 0;
+  bool wide = fi.esize == 8 && !((uintptr_t)data & 31);
+  for (int a = 1; a < fi.dims; a++)
+    if ((fi.s[a] * (int64_t)fi.esize) % 32) wide = false;
+  return kVecOk | (wide ? kVec32 : 0u);
+}
+
 // ---------------------------------------------------------------------------
 // index registry for variable-rate streams
 
@@ -482,7 +490,7 @@ size_t gpu_compress(zfp_stream* z, const zfp_field* f) {
   }
 
   Job job = base_job(fi, z, dfield);
-  job.flags = (fixed ? kFixedRate : 0u) | (vector_ok(fi, dfield) ? kVecOk : 0u);
+  job.flags = (fixed ? kFixedRate : 0u) | vector_flags(fi, dfield);
   job.words = dwords;
   job.cap_words = dcap;
   job.bit0 = bit0;
@@ -583,12 +591,29 @@ size_t gpu_decompress(zfp_stream* z, zfp_field* f) {
     if (have_index) end = ent.end_bit;
   }
 
-  // stream words
+  // stream words.  Page-locked host words are read in place, unless the
+  // tiles (on average; their sizes are known from the rate or the index)
+  // do not fit the decoder's shared memory: threads would then read their
+  // blocks word by word across the host link, far slower than one upload.
+  bool stage_stream = !stream_dev && !stream_map;
+  uint32_t want_words = 0;   // a typical tile's staged words
+  if ((fixed || have_index) && fi.nblocks) {
+    const uint64_t ntiles = (fi.nblocks + kTile - 1) / kTile;
+    const uint64_t tile_bits = fixed ? (uint64_t)kTile * z->maxbits : (end - bit0) / ntiles;
+    want_words = (uint32_t)std::min<uint64_t>(image_words(tile_bits / 64 + 4), 1u << 30);
+  }
+  if (stream_map && want_words) {
+    LaunchArgs probe;
+    std::memset(&probe, 0, sizeof probe);
+    probe.one = base_job(fi, z, f->data);
+    probe.want_words = want_words;
+    stage_stream = want_words > stage_room_any(fi.type, fi.dims, probe, false);
+  }
   DevBuf sstage;
   uint64_t* dwords = ss.begin;
   uint64_t dcap = cap_words;
   const uint64_t w_first = bit0 / 64;
-  if (!stream_dev && !stream_map) {
+  if (stage_stream) {
     const uint64_t w_end = (fixed || have_index) ? std::min<uint64_t>(cap_words, (end + 63) / 64) : cap_words;
     const uint64_t nw = w_end > w_first ? w_end - w_first : 0;
     if ((e = sstage.alloc(nw * 8, st)) != cudaSuccess) return fail_cuda("zfp_decompress: staging alloc", e);
@@ -614,7 +639,7 @@ size_t gpu_decompress(zfp_stream* z, zfp_field* f) {
   }
 
   Job job = base_job(fi, z, dfield);
-  job.flags = (fixed ? kFixedRate : 0u) | (vector_ok(fi, dfield) ? kVecOk : 0u);
+  job.flags = (fixed ? kFixedRate : 0u) | vector_flags(fi, dfield);
   job.words = dwords;
   job.cap_words = dcap;
   job.bit0 = bit0;
@@ -655,6 +680,7 @@ size_t gpu_decompress(zfp_stream* z, zfp_field* f) {
   a.njobs = 1;
   a.sc = lm.sc;
   a.one = job;
+  a.want_words = want_words;
   DevBuf gimg;
   if ((e = plan_launch(a, fi.type, fi.dims, false, fixed ? z->maxbits : bound, job.ntiles, gimg, st)) !=
       cudaSuccess)

@@ -36,6 +36,8 @@ uint32_t header_max(int type, bool rev);
 uint64_t block_bound(const FieldInfo& fi, const zfp_stream* z);
 bool is_fixed_rate(const FieldInfo& fi, const zfp_stream* z);
 bool vector_ok(const FieldInfo& fi, const void* data);
+// kVecOk, plus kVec32 where 64-bit rows are 32-byte aligned
+uint32_t vector_flags(const FieldInfo& fi, const void* data);
 Job base_job(const FieldInfo& fi, const zfp_stream* z, void* field);
 int persistent_grid();
 

@@ -17,6 +17,7 @@ enum JobFlags : uint32_t {
   kVecOk = 2u,       // full rows of 4 values can be moved with 16-byte vector accesses
   kWriteIndex = 4u,  // encode: record each block's start bit in `offsets`
   kVerify = 8u,      // decode: check every block ends where the next begins
+  kVec32 = 16u,      // with kVecOk, 64-bit rows (32 bytes) are 32-byte aligned: one access per row
 };
 
 enum JobStatus : uint32_t {

@@ -80,6 +80,9 @@ __device__ __forceinline__ void gather(const Job& job, uint64_t b, B (&raw)[1 <<
       if constexpr (sizeof(B) == 4) {
         const uint4 q = __ldg((const uint4*)row);
         raw[4 * r + 0] = q.x; raw[4 * r + 1] = q.y; raw[4 * r + 2] = q.z; raw[4 * r + 3] = q.w;
+      } else if (job.flags & kVec32) {
+        const ulonglong4_32a q = *(const ulonglong4_32a*)row;
+        raw[4 * r + 0] = q.x; raw[4 * r + 1] = q.y; raw[4 * r + 2] = q.z; raw[4 * r + 3] = q.w;
       } else {
         const ulonglong2 q0 = __ldg((const ulonglong2*)row);
         const ulonglong2 q1 = __ldg((const ulonglong2*)row + 1);
@@ -135,6 +138,12 @@ __device__ __forceinline__ void scatter(const Job& job, uint64_t b, const B (&ra
       B* row = base + y * s1 + z * s2 + w * s3;
       if constexpr (sizeof(B) == 4) {
         *(uint4*)row = make_uint4(raw[4 * r + 0], raw[4 * r + 1], raw[4 * r + 2], raw[4 * r + 3]);
+      } else if (job.flags & kVec32) {
+        // one 32-byte store per row: a warp's row stores then fill whole
+        // sectors, which matters when the field is host memory
+        ulonglong4_32a q;
+        q.x = raw[4 * r + 0]; q.y = raw[4 * r + 1]; q.z = raw[4 * r + 2]; q.w = raw[4 * r + 3];
+        *(ulonglong4_32a*)row = q;
       } else {
         ((ulonglong2*)row)[0] = make_ulonglong2(raw[4 * r + 0], raw[4 * r + 1]);
         ((ulonglong2*)row)[1] = make_ulonglong2(raw[4 * r + 2], raw[4 * r + 3]);

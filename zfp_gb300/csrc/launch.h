@@ -19,6 +19,7 @@ struct LaunchArgs {
   uint64_t* gimg;         // encode: one slot of slot_words per CTA for tiles larger than img_words
   uint32_t slot_words;
   int grid;
+  uint32_t want_words;    // decode planning: stream words a typical tile stages (0: unknown)
 };
 
 // Launchers, one explicit instantiation per (scalar type, dimensionality) in

@@ -34,11 +34,23 @@ static void prepare_kernel() {
   std::call_once(flag, [] { allow_smem(Kernel); });
 }
 
-// Dynamic shared memory one CTA of Kernel may use while as many CTAs share
-// an SM as its registers allow (at most the opt-in limit).
+// Dynamic shared memory one CTA of Kernel may use for its tile image beside
+// `planes` bytes of bit planes: the SM's shared memory split among as many
+// CTAs as its registers allow, but no more CTAs than leave each at least
+// kMinImage bytes of image (low-register 1D/2D kernels would otherwise be
+// planned with no room to stage a tile at all), nor, when a typical tile's
+// `want` bytes would not fit, more than leave room for it -- as long as
+// four CTAs still share the SM (low-register 4D decoders with large tiles).
+constexpr size_t kMinImage = 8 * 1024;
+
 template <auto Kernel>
-static size_t smem_room() {
-  static const size_t room = [] {
+static size_t smem_room(size_t planes, size_t want = 0) {
+  struct Limits {
+    int sm_smem, ctas;
+    size_t fixed;
+    bool ok;
+  };
+  static const Limits lim = [] {
     int dev = 0, sm_smem = 0, reserved = 0;
     cudaFuncAttributes fa;
     if (cudaGetDevice(&dev) != cudaSuccess ||
@@ -46,14 +58,22 @@ static size_t smem_room() {
         cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess ||
         cudaFuncGetAttributes(&fa, Kernel) != cudaSuccess) {
       cudaGetLastError();
-      return kMaxTileSmem;
+      return Limits{0, 1, 0, false};
     }
     const int regs = (fa.numRegs + 7) / 8 * 8;   // per-thread allocation granularity
     const int ctas = regs > 0 ? std::max(1, 65536 / (regs * kTile)) : 1;
-    const size_t per = (size_t)sm_smem / ctas, fixed = (size_t)reserved + fa.sharedSizeBytes;
-    return std::min(per > fixed ? per - fixed : (size_t)0, kMaxTileSmem);
+    return Limits{sm_smem, ctas, (size_t)reserved + fa.sharedSizeBytes, true};
   }();
-  return room;
+  if (!lim.ok) return kMaxTileSmem > planes ? kMaxTileSmem - planes : 0;
+  const int fit = (int)((size_t)lim.sm_smem / (planes + kMinImage + lim.fixed));
+  int ctas = std::max(1, std::min(lim.ctas, fit));
+  if (want > kMinImage && (size_t)lim.sm_smem / ctas < planes + want + lim.fixed) {
+    const int c = (int)((size_t)lim.sm_smem / (planes + want + lim.fixed));
+    if (c >= 4) ctas = std::min(ctas, c);
+  }
+  const size_t per = (size_t)lim.sm_smem / ctas;
+  const size_t room = std::min(per > lim.fixed ? per - lim.fixed : (size_t)0, kMaxTileSmem);
+  return room > planes ? room - planes : 0;
 }
 
 template <auto K> struct KernelTag { static constexpr auto kernel = K; };
@@ -110,8 +130,7 @@ uint32_t stage_room(const LaunchArgs& a, bool encode) {
   const size_t planes = encode ? plane_smem_bytes<S, D, true>(multi, a.one.maxprec)
                                : plane_smem_bytes<S, D, false>(multi, a.one.maxprec);
   auto words = [&](auto tag) -> uint32_t {
-    const size_t r = smem_room<decltype(tag)::kernel>();
-    return r > planes ? (uint32_t)((r - planes) / 8) : 0u;
+    return (uint32_t)(smem_room<decltype(tag)::kernel>(planes, encode ? 0 : (size_t)a.want_words * 8) / 8);
   };
   return encode ? with_encoder<S, D>(a, words) : with_decoder<S, D>(a, words);
 }

@@ -92,7 +92,7 @@ extern "C" size_t zfp_gb300_compress_noalloc(zfp_stream* z, const zfp_field* f) 
     return fail_cuda("zfp_gb300_compress_noalloc: clear scratch", e);
 
   Job job = base_job(fi, z, f->data);
-  job.flags = (fixed ? kFixedRate : 0u) | (vector_ok(fi, f->data) ? kVecOk : 0u);
+  job.flags = (fixed ? kFixedRate : 0u) | vector_flags(fi, f->data);
   job.words = ss.begin;
   job.cap_words = cap_words;
   job.bit0 = bit0;

@@ -337,7 +337,7 @@ uint64_t zfp_gb300_server_submit(zfp_gb300_server* s, zfp_stream* z, const zfp_f
     return 0;
   }
   Job j = base_job(fi, z, f->data);
-  j.flags = (r->fixed ? kFixedRate : 0u) | (vector_ok(fi, f->data) ? kVecOk : 0u);
+  j.flags = (r->fixed ? kFixedRate : 0u) | vector_flags(fi, f->data);
   j.words = ss.begin;
   j.cap_words = (uint64_t)(ss.end - ss.begin);
   if (direction == 0) {
