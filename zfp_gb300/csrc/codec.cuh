@@ -813,12 +813,11 @@ struct PlaneBuf {
 // Planes below the last one decoded are zero.  For 64-bit coefficients,
 // when every decoded plane lies in the top half, only the top half is
 // stored (zeros included) and `top_only` is set: the low words are zero.
-template <int P, int N, class Source, bool kWin = true>
-ZG_HD unsigned decode_planes(Source& in, unsigned budget, unsigned maxprec, PlaneBuf pb, bool& top_only) {
-  const int kmin = (unsigned)P > maxprec ? P - (int)maxprec : 0;
-  unsigned bits = budget, n = 0;
-  int k = P - 1;
-  for (; k >= kmin && bits; k--) {
+// Planes k down to klo, while budget is left, stored at pb.p[(k - kbase) *
+// pb.stride]; on return k is the first plane not decoded.
+template <int N, class Source, bool kWin>
+ZG_HD void decode_plane_range(Source& in, unsigned& bits, unsigned& n, int& k, int klo, int kbase, PlaneBuf pb) {
+  for (; k >= klo && bits; k--) {
     const unsigned m = n < bits ? n : bits;
     uint64_t x = in.read(m);
     bits -= m;
@@ -880,8 +879,16 @@ ZG_HD unsigned decode_planes(Source& in, unsigned budget, unsigned maxprec, Plan
       x |= uint64_t(1) << n;
       n++;
     }
-    pb.p[k * pb.stride] = x;
+    pb.p[(k - kbase) * pb.stride] = x;
   }
+}
+
+template <int P, int N, class Source, bool kWin = true>
+ZG_HD unsigned decode_planes(Source& in, unsigned budget, unsigned maxprec, PlaneBuf pb, bool& top_only) {
+  const int kmin = (unsigned)P > maxprec ? P - (int)maxprec : 0;
+  unsigned bits = budget, n = 0;
+  int k = P - 1;
+  decode_plane_range<N, Source, kWin>(in, bits, n, k, kmin, 0, pb);
   top_only = P == 64 && N > 4 && k >= 31;
   for (const int kz = top_only ? 32 : 0; k >= kz; k--) pb.p[k * pb.stride] = 0;
   return budget - bits;
@@ -956,13 +963,52 @@ ZG_HD unsigned decode_planes_wide(Source& in, unsigned budget, unsigned maxprec,
 // integer block codec (src/template/encode.c:260-280, decode.c:282-298,
 // revencode.c:57-79, revdecode.c:37-55)
 
+// 32 planes in slots 0-31 of pb -> 32-bit values (slot j = bit j), one
+// 32x32 transpose per 32 coefficients, loaded a transpose at a time
+template <int N>
+ZG_HD void take_half_planes(PlaneBuf pb, uint32_t (&v)[N]) {
+#pragma unroll
+  for (int grp = 0; grp < (N + 31) / 32; grp++) {
+    uint32_t a[32];
+#pragma unroll
+    for (int j = 0; j < 32; j++) a[j] = (uint32_t)(pb.p[j * pb.stride] >> (32 * grp));
+    transpose32(a);
+#pragma unroll
+    for (int i = 0; i < 32; i++)
+      if (32 * grp + i < N) v[32 * grp + i < N ? 32 * grp + i : 0] = a[i];
+  }
+}
+
 template <int D, typename I, class Source, bool kWin = true>
 ZG_HD unsigned uncode_coeffs(Source& in, unsigned budget, unsigned maxprec,
                              typename std::make_unsigned<I>::type (&u)[1 << (2 * D)], PlaneBuf pb) {
   using U = typename std::make_unsigned<I>::type;
   constexpr int N = 1 << (2 * D);
   constexpr int P = 8 * sizeof(U);
-  if constexpr (N <= 64) {
+  if constexpr (P == 64 && N == 64) {
+    // 64-bit 3D blocks: the buffer holds 32 planes.  Planes 63-32 are
+    // decoded into it and their 32-bit halves transposed at once, then the
+    // same slots take planes 31-0.
+    const int kmin = (unsigned)P > maxprec ? P - (int)maxprec : 0;
+    unsigned bits = budget, n = 0;
+    int k = P - 1;
+    decode_plane_range<N, Source, kWin>(in, bits, n, k, kmin > 32 ? kmin : 32, 32, pb);
+    for (int kk = k; kk >= 32; kk--) pb.p[(kk - 32) * pb.stride] = 0;
+    uint32_t hi[N];
+    take_half_planes<N>(pb, hi);
+    if (k >= kmin && bits) {
+      decode_plane_range<N, Source, kWin>(in, bits, n, k, kmin, 0, pb);
+      for (int kk = k; kk >= 0; kk--) pb.p[kk * pb.stride] = 0;
+      uint32_t lo[N];
+      take_half_planes<N>(pb, lo);
+#pragma unroll
+      for (int i = 0; i < N; i++) u[i] = ((U)hi[i] << 32) | lo[i];
+    } else {
+#pragma unroll
+      for (int i = 0; i < N; i++) u[i] = (U)hi[i] << 32;
+    }
+    return budget - bits;
+  } else if constexpr (N <= 64) {
     bool top_only;
     const unsigned bits = decode_planes<P, N, Source, kWin>(in, budget, maxprec, pb, top_only);
     if constexpr (P == 64 && N > 4) {

@@ -504,9 +504,18 @@ ZG_HD constexpr bool half_planes(unsigned maxprec) {
   return sizeof(typename Traits<S>::UInt) == 8 && D >= 2 && D <= 3 && maxprec <= 32;
 }
 
+// the decoder of 64-bit 3D blocks works through 32 planes at a time
+// (uncode_coeffs), whatever the job
+template <typename S, int D>
+ZG_HD constexpr bool half_decode_planes() {
+  return sizeof(typename Traits<S>::UInt) == 8 && D == 3;
+}
+
 template <typename S, int D, bool kEncode>
 ZG_HD constexpr size_t plane_smem_bytes(bool multi, unsigned maxprec) {
-  return !multi && half_planes<S, D>(maxprec) ? plane_smem_bytes<S, D, kEncode>() / 2 : plane_smem_bytes<S, D, kEncode>();
+  return (!kEncode && half_decode_planes<S, D>()) || (!multi && half_planes<S, D>(maxprec))
+             ? plane_smem_bytes<S, D, kEncode>() / 2
+             : plane_smem_bytes<S, D, kEncode>();
 }
 
 // plane k of thread 0 at planes[k * kTile]: the buffer starts at plane 32
@@ -646,7 +655,8 @@ __device__ __forceinline__ void decode_body(const Job& one, const Job* jobs, int
                                             uint32_t img_words) {
   extern __shared__ uint64_t smem_img[];
   uint64_t* img = smem_img;
-  uint64_t* planes = plane_base<S, D, kMulti>(smem_img + img_words, one);
+  uint64_t* planes = half_decode_planes<S, D>() ? smem_img + img_words
+                                                : plane_base<S, D, kMulti>(smem_img + img_words, one);
   __shared__ Job s_job;
   for (uint32_t gt = blockIdx.x; gt < total_tiles; gt += gridDim.x) {
     const Job* job = resolve_job<kMulti>(one, jobs, njobs, gt, &s_job);
