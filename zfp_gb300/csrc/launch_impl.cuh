@@ -105,6 +105,7 @@ static auto with_encoder(const LaunchArgs& a, F&& f) {
     if (five_ctas<S, D>(a.one)) return f(KernelTag<encode_kernel_occ<S, D, false, kLossyOnly, 5>>{});
     if constexpr (D == 3) return f(KernelTag<encode_kernel_occ<S, D, false, kLossyOnly, 4>>{});
   }
+  if constexpr (sizeof(S) == 8 && D == 3) return f(KernelTag<encode_kernel_occ<S, D, false, kLossyOnly, 3>>{});
   return f(KernelTag<encode_kernel<S, D, false, kLossyOnly>>{});
 }
 
