@@ -119,6 +119,47 @@ void zfp_gb300_server_free(zfp_gb300_server* server);
  * stream written here recovers block offsets by parsing the stream. */
 size_t zfp_gb300_compress_noalloc(zfp_stream* zfp, const zfp_field* field);
 
+/* ---- block indexes: zfp's index formats as a side channel ---------------
+ * A variable-rate stream carries no block offsets; zfp_decompress of one this
+ * library did not write (or no longer remembers) recovers them by parsing the
+ * stream on the GPU.  A caller holding zfp's own index of the stream -- the
+ * formats of the reference's compressed arrays, include/zfp/index.hpp --
+ * can pass it instead, and can take such an index out of a stream this
+ * library wrote.  Offsets are bit offsets from the field's first block; an
+ * index's range is the stream length in bits (hybrid indexes do not store
+ * it).  The stream must be positioned where zfp_decompress would start (after
+ * zfp_stream_rewind, or after reading a header). */
+#define ZFP_GB300_INDEX_VERBATIM 1  /* uint64 offset per block, plus the range (index.hpp:62) */
+#define ZFP_GB300_INDEX_HYBRID4  2  /* 12-byte record per 4 blocks (index.hpp:160) */
+#define ZFP_GB300_INDEX_HYBRID8  3  /* two uint64 per 8 blocks, packed for the field's dimensionality (index.hpp:307) */
+
+/* Bytes of an index of `nblocks` blocks in `format` (0: unknown format). */
+size_t zfp_gb300_index_bytes(int format, size_t nblocks);
+
+/* Pack nblocks + 1 offsets (offsets[0] = 0, offsets[nblocks] = range) into
+ * `format` (dims: the field's dimensionality, used by hybrid8).  Returns the
+ * bytes written, 0 if a block or offset is too large for the format. */
+size_t zfp_gb300_index_pack(int format, unsigned dims, const uint64_t* offsets, size_t nblocks, void* index,
+                            size_t bytes);
+
+/* Unpack an index into nblocks + 1 offsets (range: the stream length in bits,
+ * ignored for the verbatim format, which stores it). */
+zfp_bool zfp_gb300_index_unpack(int format, unsigned dims, const void* index, size_t bytes, size_t nblocks,
+                                uint64_t range, uint64_t* offsets);
+
+/* The index of the stream at zfp's position, which this library wrote for
+ * `field` (variable rate: as recorded at compression; fixed rate: from the
+ * rate).  Returns the bytes written (0 on failure); *range gets the range. */
+size_t zfp_gb300_index_export(const zfp_stream* zfp, const zfp_field* field, int format, void* index,
+                              size_t bytes, uint64_t* range);
+
+/* Let the next zfp_decompress of the stream at zfp's position use this index
+ * (same field and compression parameters) instead of parsing the stream.
+ * Every block is still checked against it while decoding; an index that
+ * does not describe the stream costs one parse, not a wrong result. */
+zfp_bool zfp_gb300_index_import(zfp_stream* zfp, const zfp_field* field, int format, const void* index,
+                                size_t bytes, uint64_t range);
+
 #ifdef __cplusplus
 }
 #endif
