@@ -726,51 +726,8 @@ ZG_HD void store_planes(const U (&u)[N], uint64_t* plane, int stride, unsigned m
 
 
 // ---------------------------------------------------------------------------
-// embedded coder for N <= 64 coefficients (one 64-bit word per plane).
-// Every output bit costs one unit of budget; see the header comment.
+// embedded plane decoder for N <= 64 coefficients (one 64-bit word per plane)
 
-template <int P, int N, class Sink>
-ZG_HD unsigned encode_planes(Sink& out, unsigned budget, unsigned maxprec, const uint64_t (&pl)[P]) {
-  const int kmin = (unsigned)P > maxprec ? P - (int)maxprec : 0;
-  unsigned bits = budget, n = 0;
-#pragma unroll
-  for (int k = P - 1; k >= 0; k--) {
-    if (k < kmin || !bits) break;
-    const uint64_t x = pl[k];
-    const unsigned m = n < bits ? n : bits;
-    out.put(x, m);
-    bits -= m;
-    if (n < (unsigned)N && bits) {
-      uint64_t r = x >> n;
-      while (bits) {
-        bits--;
-        if (!r) { out.put(0, 1); break; }        // negative group test: plane done
-        out.put(1, 1);                            // positive group test
-        const unsigned z = ctz64(r);              // zeros before the next one
-        if (n + z == (unsigned)N - 1) {           // last coefficient: its one is implied
-          const unsigned e = z < bits ? z : bits;
-          out.put(0, e);
-          bits -= e;
-          n = N;
-          break;
-        }
-        const unsigned len = z + 1, e = len < bits ? len : bits;
-        out.put(uint64_t(1) << z, e);
-        bits -= e;
-        if (e < len) break;
-        n += len;
-        r >>= len;
-      }
-    }
-  }
-  return budget - bits;
-}
-
-// Decoder twin (src/template/decode.c:80-278), rolled over planes; plane k
-// is stored to pb.p[k * pb.stride] (planes not reached are zeroed).  A
-// positive group test and the scan that follows it are read with one peek.
-// When the budget ends inside a positive group test the reference still
-// deposits a one at the scan position; so does this.
 // Whole events of a 32-bit window of group-test code that starts at a
 // positive test.  Past a plane's verbatim bits its code is a run of events
 // "1 0^z 1" (positive test, z zero scan bits, the one found) ended by a 0
@@ -806,15 +763,15 @@ struct PlaneBuf {
   int stride;
 };
 
-// kWin: decode group tests a 32-bit window at a time (event_window) where
-// the window holds whole events; measured faster for lossy blocks, which
-// have several events per plane, and slower for reversible ones, which have
-// about one per plane before every coefficient is significant.
-// Planes below the last one decoded are zero.  For 64-bit coefficients,
-// when every decoded plane lies in the top half, only the top half is
-// stored (zeros included) and `top_only` is set: the low words are zero.
-// Planes k down to klo, while budget is left, stored at pb.p[(k - kbase) *
-// pb.stride]; on return k is the first plane not decoded.
+// The decoder of src/template/decode.c:80-278, rolled over planes: planes k
+// down to klo, while budget is left, stored at pb.p[(k - kbase) *
+// pb.stride]; on return k is the first plane not decoded.  A positive group
+// test and the scan that follows it are read with one peek, or, with kWin,
+// a 32-bit window of whole events at a time (event_window): measured faster
+// for lossy blocks, which have several events per plane, and slower for
+// reversible ones, which have about one per plane before every coefficient
+// is significant.  When the budget ends inside a positive group test the
+// reference still deposits a one at the scan position; so does this.
 template <int N, class Source, bool kWin>
 ZG_HD void decode_plane_range(Source& in, unsigned& bits, unsigned& n, int& k, int klo, int kbase, PlaneBuf pb) {
   for (; k >= klo && bits; k--) {
@@ -883,6 +840,10 @@ ZG_HD void decode_plane_range(Source& in, unsigned& bits, unsigned& n, int& k, i
   }
 }
 
+// All planes of a block; planes below the last one decoded are zero.  For
+// 64-bit coefficients, when every decoded plane lies in the top half, only
+// the top half is stored (zeros included) and `top_only` is set: the low
+// words are zero.
 template <int P, int N, class Source, bool kWin = true>
 ZG_HD unsigned decode_planes(Source& in, unsigned budget, unsigned maxprec, PlaneBuf pb, bool& top_only) {
   const int kmin = (unsigned)P > maxprec ? P - (int)maxprec : 0;
