@@ -43,7 +43,7 @@ struct Job {
   uint32_t flags;           // JobFlags
   uint32_t tile0;           // first tile of this job in the launch
   uint32_t ntiles;
-  uint32_t reserved;
+  uint32_t pad;             // keeps the 64-bit fields below 8-byte aligned
   uint64_t* words;          // stream words, index 0 = beginning of the stream buffer
   uint64_t cap_words;       // words addressable at `words`
   uint64_t bit0;            // stream bit where the job's first block starts
