@@ -24,7 +24,7 @@ def host():
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.exists(nvcc):
         pytest.skip("nvcc not available")
-    deps = [SRC] + [os.path.join(HERE, "..", "zfp_gb300", "csrc", f) for f in ("codec.cuh", "kernels.cuh", "launch.h")]
+    deps = [SRC] + [os.path.join(HERE, "..", "zfp_gb300", "csrc", f) for f in ("codec.cuh", "kernels.cuh", "launch.h", "job.h")]
     if not os.path.exists(OUT) or any(os.path.getmtime(d) > os.path.getmtime(OUT) for d in deps):
         os.makedirs(os.path.dirname(OUT), exist_ok=True)
         subprocess.run([nvcc, "-std=c++17", "-O2", "-shared", "-Xcompiler", "-fPIC", "-o", OUT, SRC], check=True)
