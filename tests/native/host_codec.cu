@@ -40,6 +40,19 @@ struct VecSink {
 static bool g_or_overrun = false;
 static int g_coder = 0;   // 0: emit_block (sequential puts), 1: emit_block_2p
 
+// Kernels may give a launch's plane buffer no room below plane P - maxprec
+// (the planes a job's blocks never code).  The harness fills its plane
+// arrays with this pattern: a coder that read such a plane would produce a
+// different stream or array, and one that wrote it is recorded here.
+static const uint64_t kPlaneJunk = 0xa5a5a5a5a5a5a5a5ull;
+static bool g_floor_touched = false;
+
+static void check_floor(const uint64_t* plane, int P, unsigned maxprec, int limit) {
+  const int floor = (unsigned)P > maxprec ? P - (int)maxprec : 0;
+  for (int k = 0; k < floor && k < limit; k++)
+    if (plane[k] != kPlaneJunk) g_floor_touched = true;
+}
+
 struct OrSink {
   uint64_t* words;
   uint64_t start;
@@ -120,12 +133,14 @@ uint64_t compress_t(const Geom& g, const zg::BlockParams& p, const void* data, u
         zg::BlockHead h;
         U u[N];
         uint64_t plane[P];
+        for (int k = 0; k < P; k++) plane[k] = kPlaneJunk;
         zg::prepare_coeffs<S, D>(h, p, raw, u);
-        if (h.coded) zg::store_planes<N>(u, plane, 1, h.maxprec);
+        if (h.coded) zg::store_planes<N, true>(u, plane, 1, h.maxprec);   // as the kLossyFloor kernels
         OrSink os{words, out.pos};
         const uint64_t at = out.pos;
         const unsigned bits = zg::emit_block_2p<P, N>(out, os, h, plane, 1);
         if (os.hi > bits || out.pos != at + bits) g_or_overrun = true;
+        check_floor(plane, P, p.maxprec, P);
         continue;
       }
     }
@@ -144,7 +159,17 @@ uint64_t decompress_t(const Geom& g, const zg::BlockParams& p, void* data, const
   in.seek(bit0);
   for (size_t b = 0; b < g.blocks; b++) {
     B raw[1 << (2 * D)];
-    zg::decode_block<S, D>(in, p, raw);
+    constexpr int P = 8 * sizeof(typename zg::Traits<S>::UInt);
+    uint64_t plane[P];
+    for (int k = 0; k < P; k++) plane[k] = kPlaneJunk;
+    // lossy blocks decode as the kLossyFloor kernels do (planes below P -
+    // maxprec untouched); 64-bit 3D blocks go through 32 slots regardless
+    if (p.minexp < zg::kMinExp) {
+      zg::decode_block<S, D, zg::kRevOnly>(in, p, raw, zg::PlaneBuf{plane, 1});
+    } else {
+      zg::decode_block<S, D, zg::kLossyFloor>(in, p, raw, zg::PlaneBuf{plane, 1});
+      if (!(P == 64 && D == 3)) check_floor(plane, P, p.maxprec, P);
+    }
     size_t org[4], cnt[4];
     size_t bb = b;
     for (int a = 0; a < 4; a++) {
@@ -188,6 +213,12 @@ uint64_t decompress_s(const Geom& g, const zg::BlockParams& p, void* d, const ui
 }  // namespace
 
 extern "C" void zgh_set_coder(int c) { g_coder = c; }
+
+extern "C" int zgh_floor_touched(void) {
+  const int r = g_floor_touched;
+  g_floor_touched = false;
+  return r;
+}
 
 extern "C" int zgh_or_overrun(void) {
   const int r = g_or_overrun;

@@ -96,11 +96,13 @@ def test_device_codec_on_host_matches_oracle(host, oracle, dims, dtype, coder):
             assert e0 == e1 and np.array_equal(w0[:nw], w1[:nw]), (mode, arg, shape, trial)
             assert not host.zgh_unclean_put(), ("a sink received bits above its length", mode, arg, shape)
             assert not host.zgh_or_overrun(), ("bits written past the block's length", mode, arg, shape)
+            assert not host.zgh_floor_touched(), ("a plane below P - maxprec was written", mode, arg, shape)
             d0 = np.zeros(view.shape, dtype=dtype)
             d1 = np.zeros(view.shape, dtype=dtype)
             x0 = oracle.decompress(w0[: nw + 2], d0, prm, bit0)
             x1 = host_decompress(host, w0[: nw + 2].copy(), d1, prm, bit0)
             assert x0 == x1 and np.array_equal(d0.view(np.uint8), d1.view(np.uint8)), (mode, arg, shape, trial)
+            assert not host.zgh_floor_touched(), ("a plane below P - maxprec was written", mode, arg, shape)
 
 
 def test_integer_casts_match_fp64_arithmetic(host):

@@ -69,7 +69,9 @@ struct BlockParams {
 // Which code paths a kernel carries: both (jobs of mixed modes), or only
 // the lossy / only the reversible one -- each specialisation keeps the
 // other path's registers out of the kernel.
-enum ModeSel { kAnyMode = 0, kLossyOnly = 1, kRevOnly = 2 };
+// kLossyFloor: lossy blocks whose planes below P - maxprec have no room in
+// the plane buffer (store_planes, decode_planes and uncode_coeffs skip them)
+enum ModeSel { kAnyMode = 0, kLossyOnly = 1, kRevOnly = 2, kLossyFloor = 3 };
 
 template <int kSel>
 ZG_HD bool is_rev(const BlockParams& p) {
@@ -689,15 +691,18 @@ ZG_HD void set_half(uint64_t* p, int h, uint32_t v) {
 // no array of all planes is held in registers next to the coefficients.
 // 64-bit coefficients whose coded planes all lie in the top half
 // (maxprec <= 32: every lossy mode but high precision) transpose only their
-// high words.
-template <int N, typename U>
+// high words.  With kFloor, planes below P - maxprec (never coded) are not
+// stored: the kernel gives the buffer no room for them.
+template <int N, bool kFloor = false, typename U>
 ZG_HD void store_planes(const U (&u)[N], uint64_t* plane, int stride, unsigned maxprec = 8 * sizeof(U)) {
   constexpr int P = 8 * sizeof(U);
+  const int kmin = kFloor && (unsigned)P > maxprec ? P - (int)maxprec : 0;   // planes below are never coded
   if constexpr (N == 4) {
     uint64_t pl[P];
     make_planes<N>(u, pl);
 #pragma unroll
-    for (int k = 0; k < P; k++) plane[k * stride] = pl[k];
+    for (int k = 0; k < P; k++)
+      if (k >= kmin) plane[k * stride] = pl[k];
   } else {
     constexpr int G = (N + 31) / 32, H = P / 32;
     const bool top = P == 64 && maxprec <= 32;
@@ -715,6 +720,7 @@ ZG_HD void store_planes(const U (&u)[N], uint64_t* plane, int stride, unsigned m
         transpose32(a);
 #pragma unroll
         for (int k = 0; k < 32; k++) {
+          if (32 * half + k < kmin) continue;
           uint64_t* q = plane + (32 * half + k) * stride;
           if (G == 1) *q = a[k];
           else set_half(q, grp, a[k]);
@@ -840,18 +846,21 @@ ZG_HD void decode_plane_range(Source& in, unsigned& bits, unsigned& n, int& k, i
   }
 }
 
-// All planes of a block; planes below the last one decoded are zero.  For
-// 64-bit coefficients, when every decoded plane lies in the top half, only
-// the top half is stored (zeros included) and `top_only` is set: the low
-// words are zero.
-template <int P, int N, class Source, bool kWin = true>
+// All planes of a block; planes below the last one decoded are zero (with
+// kFloor only down to P - maxprec: the ones below are never touched, the
+// reader takes them as zero and the kernel gives them no room).  For 64-bit
+// coefficients, when every decoded plane lies in the top half, only the top
+// half is stored (zeros included) and `top_only` is set: the low words are
+// zero.
+template <int P, int N, class Source, bool kWin = true, bool kFloor = false>
 ZG_HD unsigned decode_planes(Source& in, unsigned budget, unsigned maxprec, PlaneBuf pb, bool& top_only) {
   const int kmin = (unsigned)P > maxprec ? P - (int)maxprec : 0;
   unsigned bits = budget, n = 0;
   int k = P - 1;
   decode_plane_range<N, Source, kWin>(in, bits, n, k, kmin, 0, pb);
   top_only = P == 64 && N > 4 && k >= 31;
-  for (const int kz = top_only ? 32 : 0; k >= kz; k--) pb.p[k * pb.stride] = 0;
+  const int kz = top_only ? (kFloor && kmin > 32 ? kmin : 32) : (kFloor ? kmin : 0);
+  for (; k >= kz; k--) pb.p[k * pb.stride] = 0;
   return budget - bits;
 }
 
@@ -940,7 +949,7 @@ ZG_HD void take_half_planes(PlaneBuf pb, uint32_t (&v)[N]) {
   }
 }
 
-template <int D, typename I, class Source, bool kWin = true>
+template <int D, typename I, class Source, bool kWin = true, bool kFloor = false>
 ZG_HD unsigned uncode_coeffs(Source& in, unsigned budget, unsigned maxprec,
                              typename std::make_unsigned<I>::type (&u)[1 << (2 * D)], PlaneBuf pb) {
   using U = typename std::make_unsigned<I>::type;
@@ -971,12 +980,13 @@ ZG_HD unsigned uncode_coeffs(Source& in, unsigned budget, unsigned maxprec,
     return budget - bits;
   } else if constexpr (N <= 64) {
     bool top_only;
-    const unsigned bits = decode_planes<P, N, Source, kWin>(in, budget, maxprec, pb, top_only);
+    const unsigned bits = decode_planes<P, N, Source, kWin, kFloor>(in, budget, maxprec, pb, top_only);
+    const int kmin = kFloor && (unsigned)P > maxprec ? P - (int)maxprec : 0;
     if constexpr (P == 64 && N > 4) {
       if (top_only) {
         uint64_t pl[32];
 #pragma unroll
-        for (int k = 0; k < 32; k++) pl[k] = pb.p[(32 + k) * pb.stride];
+        for (int k = 0; k < 32; k++) pl[k] = 32 + k >= kmin ? pb.p[(32 + k) * pb.stride] : 0;
         uint32_t hi[N];
         take_planes<N>(pl, hi);
 #pragma unroll
@@ -986,7 +996,7 @@ ZG_HD unsigned uncode_coeffs(Source& in, unsigned budget, unsigned maxprec,
     }
     uint64_t pl[P];
 #pragma unroll
-    for (int k = 0; k < P; k++) pl[k] = pb.p[k * pb.stride];
+    for (int k = 0; k < P; k++) pl[k] = k >= kmin ? pb.p[k * pb.stride] : 0;
     take_planes<N>(pl, u);
     return bits;
   } else {
@@ -994,13 +1004,13 @@ ZG_HD unsigned uncode_coeffs(Source& in, unsigned budget, unsigned maxprec,
   }
 }
 
-template <int D, typename I, class Source>
+template <int D, typename I, bool kFloor = false, class Source>
 ZG_HD unsigned decode_ints(Source& in, unsigned minbits, unsigned maxbits, unsigned maxprec,
                            I (&v)[1 << (2 * D)], PlaneBuf pb) {
   using U = typename std::make_unsigned<I>::type;
   constexpr int N = 1 << (2 * D);
   U u[N];
-  unsigned bits = uncode_coeffs<D, I>(in, maxbits, maxprec, u, pb);
+  unsigned bits = uncode_coeffs<D, I, Source, true, kFloor>(in, maxbits, maxprec, u, pb);
   if (bits < minbits) { in.skip_long(minbits - bits); bits = minbits; }
 #pragma unroll (N <= 64 ? N : 1)
   for (int i = 0; i < N; i++) v[perm<D>(i)] = from_nb<I>(u[i]);
@@ -1028,7 +1038,7 @@ ZG_HD unsigned rev_decode_ints(Source& in, unsigned minbits, unsigned maxbits, I
 
 ZG_HD unsigned umin(unsigned a, unsigned b) { return a < b ? a : b; }
 
-template <typename S, int D, class Source>
+template <typename S, int D, bool kFloor = false, class Source>
 ZG_HD unsigned decode_float_lossy(Source& in, const BlockParams& p,
                                   typename Traits<S>::Bits (&raw)[1 << (2 * D)], PlaneBuf pb) {
   using T = Traits<S>;
@@ -1039,7 +1049,8 @@ ZG_HD unsigned decode_float_lossy(Source& in, const BlockParams& p,
     const int emax = (int)in.read(T::kEBits) - T::kEBias;
     const unsigned maxprec = coded_precision(emax, p.maxprec, p.minexp, D);
     typename T::Int v[N];
-    bits += decode_ints<D>(in, p.minbits - umin(bits, p.minbits), p.maxbits - bits, maxprec, v, pb);
+    bits += decode_ints<D, typename T::Int, kFloor>(in, p.minbits - umin(bits, p.minbits), p.maxbits - bits,
+                                                   maxprec, v, pb);
     inv_cast<S, N>(v, raw, emax);
   } else {
 #pragma unroll (N <= 64 ? N : 1)
@@ -1599,12 +1610,13 @@ ZG_HD unsigned decode_block(Source& in, const BlockParams& p, typename Traits<S>
   using T = Traits<S>;
   constexpr int N = 1 << (2 * D);
   const bool rev = is_rev<kSel>(p);
+  constexpr bool kFloor = kSel == kLossyFloor;
   if constexpr (T::kFloat) {
-    return rev ? decode_float_rev<S, D>(in, p, raw, pb) : decode_float_lossy<S, D>(in, p, raw, pb);
+    return rev ? decode_float_rev<S, D>(in, p, raw, pb) : decode_float_lossy<S, D, kFloor>(in, p, raw, pb);
   } else {
     typename T::Int v[N];
     const unsigned bits = rev ? rev_decode_ints<D>(in, p.minbits, p.maxbits, v, pb)
-                              : decode_ints<D>(in, p.minbits, p.maxbits, p.maxprec, v, pb);
+                              : decode_ints<D, typename T::Int, kFloor>(in, p.minbits, p.maxbits, p.maxprec, v, pb);
 #pragma unroll (N <= 64 ? N : 1)
     for (int i = 0; i < N; i++) raw[i] = (typename T::Bits)v[i];
     return bits;

@@ -441,7 +441,7 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
     if constexpr (N <= 64) {
       U u[N];
       prepare_coeffs<S, D, kSel>(h, p, raw, u);
-      if (h.coded) store_planes<N>(u, my_planes, kTile, h.maxprec);
+      if (h.coded) store_planes<N, kSel == kLossyFloor>(u, my_planes, kTile, h.maxprec);
       len = fixed ? job.maxbits : block_bits<P, N>(h, my_planes, kTile);
     } else {
       prepare_coeffs<S, D, kSel>(wc.h, p, raw, wc.u);
@@ -498,10 +498,18 @@ constexpr size_t plane_smem_bytes() {
 // 32: every lossy mode but high precision) never touch planes 0-31 -- the
 // encoder transposes only the high words and the decoder keeps `top_only`
 // -- so a single-job launch gives them only the upper half of the plane
-// buffer.  Host and kernel decide it from the same job.
+// buffer.  Kernels of mode kLossyFloor (chosen for fixed-precision jobs)
+// skip every plane below P - maxprec and get maxprec planes.  Host and
+// kernel decide both from the same job.
 template <typename S, int D>
 ZG_HD constexpr bool half_planes(unsigned maxprec) {
   return sizeof(typename Traits<S>::UInt) == 8 && D >= 2 && D <= 3 && maxprec <= 32;
+}
+
+template <typename S, int D, bool kFloorKernel>
+ZG_HD constexpr unsigned plane_floor(bool multi, unsigned maxprec) {
+  constexpr unsigned P = 8 * sizeof(typename Traits<S>::UInt);
+  return multi ? 0u : kFloorKernel ? (maxprec < P ? P - maxprec : 0u) : half_planes<S, D>(maxprec) ? 32u : 0u;
 }
 
 // the decoder of 64-bit 3D blocks works through 32 planes at a time
@@ -511,18 +519,18 @@ ZG_HD constexpr bool half_decode_planes() {
   return sizeof(typename Traits<S>::UInt) == 8 && D == 3;
 }
 
-template <typename S, int D, bool kEncode>
+template <typename S, int D, bool kEncode, bool kFloorKernel = false>
 ZG_HD constexpr size_t plane_smem_bytes(bool multi, unsigned maxprec) {
-  return (!kEncode && half_decode_planes<S, D>()) || (!multi && half_planes<S, D>(maxprec))
+  constexpr unsigned P = 8 * sizeof(typename Traits<S>::UInt);
+  return !kEncode && half_decode_planes<S, D>()
              ? plane_smem_bytes<S, D, kEncode>() / 2
-             : plane_smem_bytes<S, D, kEncode>();
+             : plane_smem_bytes<S, D, kEncode>() / P * (P - plane_floor<S, D, kFloorKernel>(multi, maxprec));
 }
 
-// plane k of thread 0 at planes[k * kTile]: the buffer starts at plane 32
-// when it holds only the upper half
-template <typename S, int D, bool kMulti>
+// plane k of thread 0 at planes[k * kTile]: the buffer starts at the floor
+template <typename S, int D, bool kMulti, int kSel>
 __device__ __forceinline__ uint64_t* plane_base(uint64_t* buf, const Job& one) {
-  return !kMulti && half_planes<S, D>(one.maxprec) ? buf - 32 * kTile : buf;
+  return buf - (size_t)plane_floor<S, D, kSel == kLossyFloor>(kMulti, one.maxprec) * kTile;
 }
 
 // ---------------------------------------------------------------------------
@@ -618,7 +626,7 @@ __device__ __forceinline__ void encode_body(const Job& one, const Job* jobs, int
                                             uint32_t slot_words, uint32_t img_words) {
   extern __shared__ uint64_t smem_img[];
   uint64_t* gslot = gimg ? gimg + (size_t)blockIdx.x * slot_words : nullptr;
-  uint64_t* planes = plane_base<S, D, kMulti>(smem_img + img_words, one);
+  uint64_t* planes = plane_base<S, D, kMulti, kSel>(smem_img + img_words, one);
   __shared__ uint32_t s_tile;
   __shared__ Job s_job;
   for (uint32_t iter = blockIdx.x;; iter += gridDim.x) {
@@ -656,7 +664,7 @@ __device__ __forceinline__ void decode_body(const Job& one, const Job* jobs, int
   extern __shared__ uint64_t smem_img[];
   uint64_t* img = smem_img;
   uint64_t* planes = half_decode_planes<S, D>() ? smem_img + img_words
-                                                : plane_base<S, D, kMulti>(smem_img + img_words, one);
+                                                : plane_base<S, D, kMulti, kSel>(smem_img + img_words, one);
   __shared__ Job s_job;
   for (uint32_t gt = blockIdx.x; gt < total_tiles; gt += gridDim.x) {
     const Job* job = resolve_job<kMulti>(one, jobs, njobs, gt, &s_job);

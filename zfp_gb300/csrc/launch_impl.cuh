@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <mutex>
+#include <type_traits>
 
 #include "kernels.cuh"
 #include "launch.h"
@@ -76,21 +77,46 @@ static size_t smem_room(size_t planes, size_t want = 0) {
   return room > planes ? room - planes : 0;
 }
 
-template <auto K> struct KernelTag { static constexpr auto kernel = K; };
+// kFloor: the kernel keeps only the coded planes (mode kLossyFloor)
+template <auto K, bool kFloorPlanes = false>
+struct KernelTag {
+  static constexpr auto kernel = K;
+  static constexpr bool floor = kFloorPlanes;
+};
 
 // kernel variant: device job array -> multi-job kernel carrying both mode
-// paths; a single job -> the variant of its mode only
+// paths; a single job -> the variant of its mode only.
 // A 32-bit fixed-rate tile small enough for a fifth of an SM's shared memory
-// (with the bit planes) goes to the five-CTA kernels.  Decided from the job
-// alone, so planning and launching pick the same kernel.
+// (with the bit planes) goes to the five-CTA kernels; so does a 32-bit
+// fixed-precision job whose largest tile fits there beside only its coded
+// planes (the kLossyFloor kernels: precision up to about 20).  Decided from
+// the job alone, so planning and launching pick the same kernel.
+constexpr size_t kFifthShare = 228 * 1024 / 5 - 2048;   // per CTA, less reserved and static memory
+
 template <typename S, int D>
 static bool five_ctas(const Job& j) {
   if constexpr (sizeof(S) != 4 || D > 3) {
     return false;
   } else {
-    constexpr size_t kShare = 228 * 1024 / 5 - 2048;   // per CTA, less reserved and static memory
     const size_t tile = image_words((uint64_t)kTile * j.maxbits / 64 + 4) * 8 + plane_smem_bytes<S, D, false>();
-    return (j.flags & kFixedRate) && tile <= kShare;
+    return (j.flags & kFixedRate) && tile <= kFifthShare;
+  }
+}
+
+template <typename S, int D>
+static bool five_ctas_floor(const Job& j) {
+  if constexpr (sizeof(S) != 4 || D > 3) {
+    return false;
+  } else {
+    // bits of one block at most (block_bound): the header and every coded plane
+    constexpr uint64_t N = 1u << (2 * D), P = 32, hm = std::is_floating_point<S>::value ? 1 + 8 : 0;
+    if ((j.flags & kFixedRate) || j.maxprec >= P) return false;
+    uint64_t b = hm + N - 1 + N * (uint64_t)j.maxprec;
+    if (j.maxbits >= hm) b = std::min<uint64_t>(b, j.maxbits);
+    b = std::max<uint64_t>(b, j.minbits);
+    const size_t tile =
+        image_words((uint64_t)kTile * b / 64 + 4) * 8 + plane_smem_bytes<S, D, false, true>(false, j.maxprec);
+    return tile <= kFifthShare;
   }
 }
 
@@ -102,6 +128,7 @@ static auto with_encoder(const LaunchArgs& a, F&& f) {
     else return f(KernelTag<encode_kernel<S, D, false, kRevOnly>>{});
   }
   if constexpr (sizeof(S) == 4 && D <= 3) {
+    if (five_ctas_floor<S, D>(a.one)) return f(KernelTag<encode_kernel_occ<S, D, false, kLossyFloor, 5>, true>{});
     if (five_ctas<S, D>(a.one)) return f(KernelTag<encode_kernel_occ<S, D, false, kLossyOnly, 5>>{});
     if constexpr (D == 3) return f(KernelTag<encode_kernel_occ<S, D, false, kLossyOnly, 4>>{});
   }
@@ -119,28 +146,34 @@ static auto with_decoder(const LaunchArgs& a, F&& f) {
   if constexpr (sizeof(S) == 8 && D <= 3) {
     return f(KernelTag<decode_kernel_occ<S, D, false, kLossyOnly, 3>>{});
   } else {
+    if (five_ctas_floor<S, D>(a.one)) return f(KernelTag<decode_kernel_occ<S, D, false, kLossyFloor, 5>, true>{});
     if (five_ctas<S, D>(a.one)) return f(KernelTag<decode_kernel_occ<S, D, false, kLossyOnly, 5>>{});
     if constexpr (sizeof(S) == 4 && D == 3) return f(KernelTag<decode_kernel_occ<S, D, false, kLossyOnly, 4>>{});
     else return f(KernelTag<decode_kernel<S, D, false, kLossyOnly>>{});
   }
 }
 
+// plane-buffer bytes the chosen kernel keeps
+template <typename S, int D, bool kEncode, class Tag>
+static size_t planes_of(const LaunchArgs& a) {
+  return plane_smem_bytes<S, D, kEncode, Tag::floor>(a.jobs != nullptr, a.one.maxprec);
+}
+
 template <typename S, int D>
 uint32_t stage_room(const LaunchArgs& a, bool encode) {
-  const bool multi = a.jobs != nullptr;
-  const size_t planes = encode ? plane_smem_bytes<S, D, true>(multi, a.one.maxprec)
-                               : plane_smem_bytes<S, D, false>(multi, a.one.maxprec);
   auto words = [&](auto tag) -> uint32_t {
-    return (uint32_t)(smem_room<decltype(tag)::kernel>(planes, encode ? 0 : (size_t)a.want_words * 8) / 8);
+    using Tag = decltype(tag);
+    const size_t planes = encode ? planes_of<S, D, true, Tag>(a) : planes_of<S, D, false, Tag>(a);
+    return (uint32_t)(smem_room<Tag::kernel>(planes, encode ? 0 : (size_t)a.want_words * 8) / 8);
   };
   return encode ? with_encoder<S, D>(a, words) : with_decoder<S, D>(a, words);
 }
 
 template <typename S, int D>
 cudaError_t run_encode(const LaunchArgs& a, cudaStream_t st) {
-  const size_t smem = (size_t)a.img_words * 8 + plane_smem_bytes<S, D, true>(a.jobs != nullptr, a.one.maxprec);
   return with_encoder<S, D>(a, [&](auto tag) {
     constexpr auto kernel = decltype(tag)::kernel;
+    const size_t smem = (size_t)a.img_words * 8 + planes_of<S, D, true, decltype(tag)>(a);
     prepare_kernel<kernel>();
     kernel<<<a.grid, kTile, smem, st>>>(a.one, a.jobs, a.njobs, a.sc, a.total_tiles, a.use_ticket, a.gimg,
                                         a.slot_words, a.img_words);
@@ -150,9 +183,9 @@ cudaError_t run_encode(const LaunchArgs& a, cudaStream_t st) {
 
 template <typename S, int D>
 cudaError_t run_decode(const LaunchArgs& a, cudaStream_t st) {
-  const size_t smem = (size_t)a.img_words * 8 + plane_smem_bytes<S, D, false>(a.jobs != nullptr, a.one.maxprec);
   return with_decoder<S, D>(a, [&](auto tag) {
     constexpr auto kernel = decltype(tag)::kernel;
+    const size_t smem = (size_t)a.img_words * 8 + planes_of<S, D, false, decltype(tag)>(a);
     prepare_kernel<kernel>();
     kernel<<<a.grid, kTile, smem, st>>>(a.one, a.jobs, a.njobs, a.total_tiles, a.img_words);
     return cudaGetLastError();
