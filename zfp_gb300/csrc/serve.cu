@@ -56,9 +56,11 @@ struct Lane {
   std::vector<std::shared_ptr<Request>> reqs;
   void* dev = nullptr;           // jobs, scratch, results, index of the running batch
   JobResult* host_results = nullptr;   // pinned
-  size_t host_cap = 0;
   Job* host_jobs = nullptr;      // pinned staging for the job arrays
   size_t host_jobs_cap = 0;
+  // outgrown staging buffers, freed with the server: cudaFreeHost waits for
+  // the whole device, which would stall every lane in the middle of serving
+  std::vector<void*> retired;
   std::vector<size_t> index_off; // per request: offset of its block index in `dev` (compress, variable rate)
   struct Server* server = nullptr;
 };
@@ -75,6 +77,25 @@ struct Server {
   uint64_t next_ticket = 1;
   int device = 0;
 };
+
+// pinned staging for `cap` jobs and results; the old buffers are retired
+// (freed with the server), not freed now
+static cudaError_t grow_staging(Lane* lane, size_t cap) {
+  Job* jobs = nullptr;
+  JobResult* results = nullptr;
+  cudaError_t e = cudaHostAlloc((void**)&jobs, cap * sizeof(Job), 0);
+  if (e != cudaSuccess) return e;
+  if ((e = cudaHostAlloc((void**)&results, cap * sizeof(JobResult), 0)) != cudaSuccess) {
+    lane->retired.push_back(jobs);
+    return e;
+  }
+  if (lane->host_jobs) lane->retired.push_back(lane->host_jobs);
+  if (lane->host_results) lane->retired.push_back(lane->host_results);
+  lane->host_jobs = jobs;
+  lane->host_results = results;
+  lane->host_jobs_cap = cap;
+  return cudaSuccess;
+}
 
 static void CUDART_CB lane_done(void* arg) {
   Lane* lane = (Lane*)arg;
@@ -132,12 +153,7 @@ static cudaError_t launch_batch(Server* s, Lane* lane) {
   // host staging for job arrays and results
   size_t njobs = reqs.size();
   if (lane->host_jobs_cap < njobs) {
-    if (lane->host_jobs) cudaFreeHost(lane->host_jobs);
-    lane->host_jobs_cap = std::max<size_t>(njobs, 256);
-    if ((e = cudaHostAlloc((void**)&lane->host_jobs, lane->host_jobs_cap * sizeof(Job), 0)) != cudaSuccess) return e;
-    if (lane->host_results) cudaFreeHost(lane->host_results);
-    if ((e = cudaHostAlloc((void**)&lane->host_results, lane->host_jobs_cap * sizeof(JobResult), 0)) != cudaSuccess)
-      return e;
+    if ((e = grow_staging(lane, std::max<size_t>(njobs, 2 * lane->host_jobs_cap))) != cudaSuccess) return e;
   }
   size_t hj = 0;
   for (auto& g : gs) {
@@ -305,6 +321,9 @@ zfp_gb300_server* zfp_gb300_server_create(size_t hbm_budget, int lanes) {
       delete s;
       return nullptr;
     }
+    // staging for batches of up to 1024 requests, allocated now rather than
+    // while serving (a failure here is retried when a batch needs it)
+    if (grow_staging(l.get(), 1024) != cudaSuccess) cudaGetLastError();
     s->lanes.push_back(std::move(l));
   }
   s->worker = std::thread(dispatcher, s);
@@ -410,6 +429,7 @@ void zfp_gb300_server_free(zfp_gb300_server* s) {
     cudaStreamSynchronize(l->st);
     if (l->host_jobs) cudaFreeHost(l->host_jobs);
     if (l->host_results) cudaFreeHost(l->host_results);
+    for (void* p : l->retired) cudaFreeHost(p);
     cudaStreamDestroy(l->st);
   }
   delete s;
