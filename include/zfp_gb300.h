@@ -111,12 +111,16 @@ void zfp_gb300_server_free(zfp_gb300_server* server);
  * device array inside the library (held by every GPU that loads it), which
  * limits a call to 4,194,304 zfp blocks (e.g. 512^3 float) and to blocks
  * whose tile fits shared memory.  Larger or host-resident inputs return 0
- * with a reason in zfp_gb300_last_error().  The first call on a device
- * looks up that array's device address; make that first call before any
- * CUDA stream capture.  All calls share the array: calls whose GPU work
- * overlaps (other CUDA streams or host threads) race and must be ordered by
- * the caller.  No block index is kept, so zfp_decompress of a variable-rate
- * stream written here recovers block offsets by parsing the stream. */
+ * with a reason in zfp_gb300_last_error().  The first call on a device (in
+ * each CUDA context of it) does a set-up step: it looks up that array's
+ * device address.  Make that first call before any CUDA stream capture
+ * begins.  Each call waits for its own GPU work before it returns.  All
+ * calls share the array, which keeps the last call's contents (each call
+ * clears what it uses): calls whose GPU work overlaps (other CUDA streams or
+ * host threads) race and must be ordered by the caller.  No block index is
+ * kept, and one kept for an earlier stream at the same place is dropped, so
+ * zfp_decompress of a variable-rate stream written here recovers block
+ * offsets by parsing the stream. */
 size_t zfp_gb300_compress_noalloc(zfp_stream* zfp, const zfp_field* field);
 
 /* ---- block indexes: zfp's index formats as a side channel ---------------

@@ -41,14 +41,59 @@ def build(quiet: bool = True) -> str:
     return LIB_PATH
 
 
-def build_ref(quiet: bool = True) -> str | None:
-    """Compile the reference library from its sources, if they are present here."""
-    if not os.path.isdir("/root/reference/src"):
-        return REF_LIB_PATH if os.path.exists(REF_LIB_PATH) else None
-    out = subprocess.run(["make", "-C", HERE, "ref"], capture_output=quiet, text=True)
+REF_CUDA_LIB_PATH = os.path.join(HERE, "_ref", "libzfp_refcuda.so")
+STAGED = os.path.join(HERE, "_ref", "src")
+
+
+def reference_checkout() -> str | None:
+    """The reference's source checkout on this machine: $ZFP_REFERENCE, else
+    the recipe's default location (absent on the GPU host)."""
+    for d in (os.environ.get("ZFP_REFERENCE"), "/root/reference"):
+        if d and os.path.isfile(os.path.join(d, "src", "zfp.c")):
+            return d
+    return None
+
+
+def reference_sources() -> str | None:
+    """Where the reference's sources can be compiled from: the checkout, or
+    the copy `make stage` put under oracle/_ref/src (git-ignored)."""
+    d = reference_checkout()
+    if d:
+        return d
+    return STAGED if os.path.isfile(os.path.join(STAGED, "src", "zfp.c")) else None
+
+
+def stage_ref(quiet: bool = True) -> bool:
+    """Copy the reference sources the recipe compiles into oracle/_ref/src, so
+    that they travel with the working tree to a machine without a checkout."""
+    if not reference_checkout():
+        return False
+    out = subprocess.run(["make", "-C", HERE, "stage"], capture_output=quiet, text=True)
     if out.returncode != 0:
-        raise RuntimeError("reference build failed:\n" + (out.stdout or "") + (out.stderr or ""))
-    return REF_LIB_PATH
+        raise RuntimeError("staging the reference sources failed:\n" + (out.stdout or "") + (out.stderr or ""))
+    return True
+
+
+def _make(target: str, path: str, quiet: bool) -> str | None:
+    src = reference_sources()
+    if not src:
+        return path if os.path.exists(path) else None
+    jobs = str(min(32, os.cpu_count() or 4))
+    out = subprocess.run(["make", "-j", jobs, "-C", HERE, target, f"ZFP_REFERENCE={src}"],
+                         capture_output=quiet, text=True)
+    if out.returncode != 0:
+        raise RuntimeError(f"reference build ({target}) failed:\n" + (out.stdout or "") + (out.stderr or ""))
+    return path
+
+
+def build_ref(quiet: bool = True) -> str | None:
+    """Compile the reference library (serial + OpenMP codecs) from its sources, where they are present."""
+    return _make("ref", REF_LIB_PATH, quiet)
+
+
+def build_ref_cuda(quiet: bool = True) -> str | None:
+    """Compile the reference library with its own CUDA backend (src/cuda_zfp) for sm_103a."""
+    return _make("refcuda", REF_CUDA_LIB_PATH, quiet)
 
 
 def mode_params(mode: str, arg=None, dtype=np.float32, dims: int = 3, align: bool = False):

@@ -158,7 +158,7 @@ def main():
                                       "mode": mode, "arg": arg, "layout": layout, "header": header,
                                       "header_bits": int(hbits), "params": list(prm),
                                       "decoded_sha256": hashlib.sha256(out.tobytes()).hexdigest()})
-    # BASELINE configuration 1: 3D float64 64^3 smooth field, seed 0, N(0,1e-3), fixed rate 16
+    # plain-codec configuration: 3D float64 64^3 smooth field, seed 0, N(0,1e-3), fixed rate 16
     c1 = synth.smooth_field((64, 64, 64), np.float64, seed=0, noise=1e-3)
     arrays["in_config1"] = c1
     stream, out, prm, _ = ref_run(ref, c1, "rate", 16, False)

@@ -34,11 +34,8 @@ struct VecSink {
   ZG_HD void finish() {}
 };
 
-// Positional sink for zg::emit_block_2p: ORs v (n bits, clean) at
-// bit start + pos.  Writes at or past `end` (the block's returned length,
-// checked after the block) are recorded as overruns.
-static bool g_or_overrun = false;
-static int g_coder = 0;   // 0: emit_block (sequential puts), 1: emit_block_2p
+static bool g_or_overrun = false;   // the kernel's coder wrote past the length it returned
+static int g_coder = 0;   // 0: emit_block (one put per significance event), 1: emit_block_seq (table coder)
 
 // Kernels may give a launch's plane buffer no room below plane P - maxprec
 // (the planes a job's blocks never code).  The harness fills its plane
@@ -52,24 +49,6 @@ static void check_floor(const uint64_t* plane, int P, unsigned maxprec, int limi
   for (int k = 0; k < floor && k < limit; k++)
     if (plane[k] != kPlaneJunk) g_floor_touched = true;
 }
-
-struct OrSink {
-  uint64_t* words;
-  uint64_t start;
-  uint64_t hi = 0;        // one past the highest bit written
-  ZG_HD void set(uint64_t pos, uint64_t v, unsigned n) {
-#if !defined(__CUDA_ARCH__)
-    if (n < 64 && (v >> n)) g_unclean_put = true;
-#endif
-    if (!n) return;
-    const uint64_t a = start + pos;
-    const unsigned o = (unsigned)(a & 63);
-    words[a >> 6] |= v << o;
-    if (o && o + n > 64) words[(a >> 6) + 1] |= v >> (64 - o);
-    if (pos + n > hi) hi = pos + n;
-  }
-  ZG_HD void set_small(uint64_t pos, unsigned v, unsigned n) { set(pos, v, n); }
-};
 
 struct Geom {
   int dims;
@@ -136,10 +115,9 @@ uint64_t compress_t(const Geom& g, const zg::BlockParams& p, const void* data, u
         for (int k = 0; k < P; k++) plane[k] = kPlaneJunk;
         zg::prepare_coeffs<S, D>(h, p, raw, u);
         if (h.coded) zg::store_planes<N, true>(u, plane, 1, h.maxprec);   // as the kLossyFloor kernels
-        OrSink os{words, out.pos};
         const uint64_t at = out.pos;
-        const unsigned bits = zg::emit_block_2p<P, N>(out, os, h, plane, 1);
-        if (os.hi > bits || out.pos != at + bits) g_or_overrun = true;
+        const unsigned bits = zg::emit_block_seq<P, N>(out, h, plane, 1, zg::kGroupCodeHost.e);
+        if (out.pos != at + bits) g_or_overrun = true;
         check_floor(plane, P, p.maxprec, P);
         continue;
       }

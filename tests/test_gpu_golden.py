@@ -1,6 +1,6 @@
 """GPU streams and decoded arrays against the reference library's own
 outputs (tests/golden, written by tests/golden/make_golden.py), including
-streams that follow a full zfp header and BASELINE configuration 1
+streams that follow a full zfp header and the plain-codec configuration
 (3D float64 64^3, fixed rate 16)."""
 from __future__ import annotations
 

@@ -63,14 +63,14 @@ SPECIAL = {np.float32: np.array([0.0, -0.0, 1e-45, -1e-45, 1e-40, 3.4e38, -3.4e3
                                  1.0, -2.5, 1e-300, 1e-290])}
 
 
-@pytest.mark.parametrize("coder", ["sequential", "positional"])
+@pytest.mark.parametrize("coder", ["per_event", "table"])
 @pytest.mark.parametrize("dims", [1, 2, 3, 4])
 @pytest.mark.parametrize("dtype", [np.float32, np.float64, np.int32, np.int64], ids=lambda d: np.dtype(d).name)
 def test_device_codec_on_host_matches_oracle(host, oracle, dims, dtype, coder):
-    """Both plane coders of codec.cuh: emit_block (sequential puts) and
-    emit_block_2p (a sequential pass plus a pass that ORs event bits at
-    computed positions, used by the encoder kernel for 1-3D blocks)."""
-    host.zgh_set_coder(1 if coder == "positional" else 0)
+    """Both plane coders of codec.cuh: emit_block (one put per significance
+    event) and emit_block_seq (group-test codes a byte at a time from a
+    table, used by the encoder kernel for 1-3D blocks)."""
+    host.zgh_set_coder(1 if coder == "table" else 0)
     rng = np.random.default_rng(dims * 10 + ZTYPE[np.dtype(dtype)])
     modes = [("rate", 4), ("rate", 12.5), ("rate", 1), ("precision", 7), ("precision", 20), ("accuracy", 1e-3),
              ("accuracy", 1e-9), ("reversible", None), ("rate", 32), ("precision", 64), ("expert", (30, 70, 33, -5))]

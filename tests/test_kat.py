@@ -10,7 +10,7 @@ fixed precision 2^(p+3), fixed rate 2^(p+3) (unaligned), fixed accuracy
 2^-(2^p) for p = 0, 1, 2, and reversible.  For every table entry of an
 end-to-end array test, the oracle's stream (its flushed bytes) and decoded
 array must hash to the recorded value.  CPU only; needs the reference's
-sources (skipped where they are absent)."""
+sources (its checkout, or the copy staged from it; skipped where neither exists)."""
 from __future__ import annotations
 
 import ctypes as C
@@ -22,9 +22,9 @@ import subprocess
 import numpy as np
 import pytest
 
-from oracle.pyoracle import mode_params
+from oracle.pyoracle import mode_params, reference_sources
 
-REF = "/root/reference"
+REF = reference_sources() or ""
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.join(os.path.dirname(HERE), "oracle")
 KAT_LIB = os.path.join(ORACLE, "_ref", "libzfpkat.so")
@@ -36,9 +36,9 @@ MODES = {"rate": 2, "precision": 3, "accuracy": 4, "reversible": 5}   # zfp_mode
 
 @pytest.fixture(scope="module")
 def kat():
-    if not os.path.isdir(os.path.join(REF, "tests", "utils")):
+    if not REF or not os.path.isdir(os.path.join(REF, "tests", "utils")):
         pytest.skip("reference sources not available here")
-    r = subprocess.run(["make", "-C", ORACLE, "kat"], capture_output=True, text=True)
+    r = subprocess.run(["make", "-C", ORACLE, "kat", f"ZFP_REFERENCE={REF}"], capture_output=True, text=True)
     if r.returncode != 0:
         pytest.skip("reference test utilities do not build here: " + r.stderr[-300:])
     lib = C.CDLL(KAT_LIB)

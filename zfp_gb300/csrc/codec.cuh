@@ -1,7 +1,7 @@
 // codec.cuh -- zfp fixed-/variable-rate block codec, one zfp block per thread.
 //
 // Everything here is __host__ __device__ so the per-block logic can be run on
-// the CPU against the oracle; the kernels (encode.cu / decode.cu) supply the
+// the CPU against the oracle; the kernels (kernels.cuh) supply the
 // bit sinks/sources, gather/scatter and the stream assembly.
 //
 // Design (GB300-first, not a translation of src/cuda_zfp):
@@ -10,8 +10,9 @@
 //    compile time);
 //  * bit planes are formed by a register bit-matrix transpose (byte-permute
 //    for the 16/8-bit levels, masked swaps below) instead of per-bit loops;
-//  * group tests are coded one significance event at a time with
-//    count-trailing-zeros, never bit by bit;
+//  * group tests are coded a byte of coefficient bits at a time from a
+//    table (emit_block_seq) and decoded a window of whole events at a
+//    time (event_window), never bit by bit;
 //  * the rate-limited and whole-plane coders of the reference are one coder
 //    here: the rate-limited stream is the whole-plane stream cut at maxbits
 //    (src/template/encode.c:92-256), which is exactly what a per-bit budget
@@ -1352,117 +1353,123 @@ ZG_HD unsigned emit_block(Sink& out, const BlockHead& h, const uint64_t* plane, 
   return bits;
 }
 
-// Two-pass coder (N <= 64) for kernels that own a zeroed image.  Every
-// plane's code starts at an offset known from the O(1) plane lengths:
-//  pass 1, through the sequential sink `seq`: per plane the n verbatim bits
-//    and, if anything above n is set, the opening positive group test; the
-//    rest of the plane's code is skipped (pad) and filled in by pass 2.
-//    Planes with such bits ("event planes") are remembered: the slot of
-//    plane k is overwritten with r = x >> n, a flag for an implied last one
-//    and the block-relative bit b = start + n + 1 (r << 16 | flag << 15 | b;
-//    the one plane a block may have with r >= 2^48 keeps flag and b in a
-//    register);
-//  pass 2, one flat loop over every one bit of every event plane, through
-//    the positional sink `pos` (out.set_small(at, v, n): OR v, n bits, at
-//    the block-relative bit `at`).  The j-th one at offset p of r sits at
-//    b + p + j and, unless it is the plane's last one, is followed by a
-//    positive test; a last one at the last coefficient is implied and not
-//    written.  A new event plane costs pass 2 one shared-memory load.
-// Zeros need no writes, and bits at or past the budget are dropped, which
-// cuts the code exactly where the reference's bit budget stops the coder
-// (src/template/encode.c:92-256).  Pass 2 runs once per event of the block
-// rather than once per event inside a loop per plane, so the lanes of a warp
-// diverge far less.  Returns the block's bits, as emit_block.
-template <int P, int N, class Seq, class Pos>
-ZG_HD unsigned emit_block_2p(Seq& seq, Pos& pos, const BlockHead& h, uint64_t* plane, int stride) {
-  using Mask = typename std::conditional<(P <= 32), uint32_t, uint64_t>::type;
-  seq.put(h.hdr, h.hdr_bits);
+// ---------------------------------------------------------------------------
+// Table-driven sequential coder (N <= 64).
+//
+// Past its n verbatim bits, plane x's code is a pure function of r = x >> n
+// (src/template/encode.c:92-132): a positive test '1' if r != 0 (else a
+// single '0'), then r's bits from the bottom up to its top one, each one
+// followed by a test bit -- '1' (more ones follow) or, after the last one,
+// '0'.  A last one at coefficient N-1 is implied: neither it nor a test
+// after it is written.  So the code of r is the expansion E(r) of r in
+// which every one becomes '11', with the bit after the last one cleared or
+// the last one's two bits dropped.  E is computed a byte at a time from a
+// 256-entry table (group_code_entry): E(b) with popc(b) above it; a 16-bit
+// chunk of r is two lookups, whatever its number of ones.  The coder walks
+// the planes in one flat loop whose iterations each start a plane (its
+// verbatim bits and opening test: one put) and code one 16-bit chunk of its
+// r (one put); most planes need one iteration.  Every put is cut at the bit
+// budget, which truncates the code exactly where the reference's per-bit
+// budget stops its coder (src/template/encode.c:92-256).
+
+// E(b) in bits 0-15 (every one of the byte b followed by a '1'), popc(b) in bits 16-19
+ZG_HD constexpr uint32_t group_code_entry(uint32_t b) {
+  uint32_t e = 0, j = 0;
+  for (uint32_t p = 0; p < 8; p++)
+    if ((b >> p) & 1u) {
+      e |= 3u << (p + j);
+      j++;
+    }
+  return e | (j << 16);
+}
+
+struct GroupCodeTable {
+  uint32_t e[256];
+};
+
+constexpr GroupCodeTable make_group_code_table() {
+  GroupCodeTable t{};
+  for (uint32_t b = 0; b < 256; b++) t.e[b] = group_code_entry(b);
+  return t;
+}
+
+constexpr GroupCodeTable kGroupCodeHost = make_group_code_table();
+
+template <int P, int N, class Sink>
+ZG_HD unsigned emit_block_seq(Sink& out, const BlockHead& h, const uint64_t* plane, int stride, const uint32_t* gtab) {
+  out.put(h.hdr, h.hdr_bits);
   unsigned bits = h.hdr_bits;
-  Mask events = 0;                        // bit k: plane k has ones above its n
-  int wide_k = -1;                        // the event plane whose r needs all 64 bits, if any
-  unsigned wide_meta = 0;
-  // positions fit 16 bits: a block's code is at most P * (N + 2) + N bits
-  unsigned lim = 0;
   if (h.coded) {
     const int kmin = (unsigned)P > h.maxprec ? P - (int)h.maxprec : 0;
-    const uint64_t lim64 = (uint64_t)h.hdr_bits + h.budget;  // first dropped position
-    lim = lim64 < 0xffffu ? (unsigned)lim64 : 0xffffu;
-    unsigned at = h.hdr_bits;                                // start of the current plane's code
-    unsigned n = 0;
+    unsigned left = h.budget;        // bits the plane coder may still write
+    unsigned n = 0;                  // coefficients already significant
     int k = P - 1;
-    for (; k >= kmin && at < lim && n < (unsigned)N; k--) {
-      const uint64_t x = plane[k * stride];
-      const unsigned n0 = n;
-      const unsigned len = plane_bits<N>(x, n);
-      const unsigned room = len < lim - at ? len : lim - at;
-      const unsigned m = n0 < room ? n0 : room;
-      const unsigned ev = n != n0 && room > m;               // opening positive test of an event plane
-      seq.put(low_bits(x, m) | ((uint64_t)ev << m), m + ev);
-      if (ev) {
-        // pass 2 finds the plane's ones, whether the last one is implied
-        // and where the first one's position is counted from (a block's
-        // code is under 2^15 bits) in the plane's slot: r << 16 | meta.
-        // At most one plane has r >= 2^48 (it needs n < 16 before and
-        // leaves n > 48): its slot holds r, its meta a register.
-        const uint64_t r = x >> n0;
-        const unsigned meta = ((unsigned)(n >= (unsigned)N) << 15) | (at + n0 + 1);
-        if (!(r >> 48)) {
-          plane[k * stride] = (r << 16) | meta;
-        } else {
-          plane[k * stride] = r;
-          wide_k = k;
-          wide_meta = meta;
+    uint64_t r = 0;                  // group-test bits of the current plane not yet coded (next chunk at bit 0)
+    int rem = -1;                    // position in r of the plane's last one; -1: none pending
+    bool implied = false;            // that one is coefficient N-1
+    while (left) {
+      if (rem < 0) {                 // next plane: verbatim bits and the opening test
+        if (k < kmin) break;
+        const uint64_t x = plane[k * stride];
+        k--;
+        uint64_t v = x;
+        unsigned len = N;
+        if (n < (unsigned)N) {
+          const uint64_t g = x >> n;
+          v = low_bits(x, n) | ((uint64_t)(g != 0) << n);
+          len = n + 1;
+          if (g) {
+            const unsigned top = 63u - (unsigned)clz64(g);
+            implied = n + top == (unsigned)N - 1;
+            rem = (int)top;
+            r = g;
+            n += top + 1;
+          }
         }
-        events |= Mask(1) << k;
+        if (len >= left) {
+          out.put(low_bits(v, left), left);
+          left = 0;
+          break;
+        }
+        out.put(v, len);
+        left -= len;
+        if (rem < 0) continue;
       }
-      seq.pad(room - m - ev);
-      at += len;
-    }
-    // once every coefficient is significant a plane is its N bits, verbatim:
-    // whole 64-bit planes first (a constant-width put), then one cut plane
-    if constexpr (N == 64) {
-      for (; k >= kmin && at + 64u <= lim; k--) {
-        seq.put(plane[k * stride], 64);
-        at += 64;
+      // the next 16 bits of r
+      const uint32_t c = (uint32_t)r & 0xffffu;
+      const uint32_t e0 = gtab[c & 0xffu], e1 = gtab[c >> 8];
+      const unsigned p0 = e0 >> 16, pc = p0 + (e1 >> 16);
+      uint32_t code = (e0 & 0xffffu) | ((e1 & 0xffffu) << (8 + p0));
+      unsigned len = 16 + pc;
+      if (rem < 16) {                // the plane's last chunk: up to its last one
+        if (implied) {
+          len = (unsigned)rem + pc - 1;                 // the one and its test are not written
+          code &= len < 32 ? (1u << len) - 1 : ~0u;
+        } else {
+          len = (unsigned)rem + pc + 1;                 // the test after the last one is negative
+          code &= ~(1u << (len - 1));
+        }
+        rem = -1;
+      } else {
+        r >>= 16;
+        rem -= 16;
       }
+      if (len >= left) {
+        out.put(low_bits(code, left), left);
+        left = 0;
+        break;
+      }
+      out.put(code, len);
+      left -= len;
     }
-    for (; k >= kmin && at < lim; k--) {
-      const unsigned m = lim - at < (unsigned)N ? lim - at : (unsigned)N;
-      seq.put(low_bits(plane[k * stride], m), m);
-      at += N;
-    }
-    bits += (at < lim ? at : lim) - h.hdr_bits;
+    bits += h.budget - left;
   }
   if (bits < h.pad_to) {
-    seq.pad(h.pad_to - bits);
+    out.pad(h.pad_to - bits);
     bits = h.pad_to;
-  }
-  seq.finish();
-  uint64_t r = 0;
-  unsigned b = 0;                           // the j-th one at offset p of r sits at b + p + j
-  bool implied = false;
-  while (r || events) {
-    if (!r) {
-      const int k = 63 - clz64((uint64_t)events);
-      events &= ~(Mask(1) << k);
-      const uint64_t v = plane[k * stride];
-      const bool wide = k == wide_k;
-      r = wide ? v : v >> 16;
-      const unsigned meta = wide ? wide_meta : (unsigned)v;
-      implied = (meta >> 15) & 1;
-      b = meta & 0x7fffu;
-    }
-    const unsigned p = b + ctz64(r);
-    r &= r - 1;
-    b++;
-    if (p < lim) {
-      if (r) pos.set_small(p, p + 1 < lim ? 3u : 1u, p + 1 < lim ? 2u : 1u);   // the one, then a positive test
-      else if (!implied) pos.set_small(p, 1u, 1u);                          // the plane's last one
-    }
   }
   return bits;
 }
-
 
 // 4D blocks keep the rolled wide coder over the coefficient array
 template <typename S>

@@ -278,15 +278,31 @@ IndexEntry make_entry(const void* begin, uint64_t bit0, uint64_t end_bit, const 
   return e;
 }
 
+// Indexes dropped by calls that must not free device memory (the no-alloc
+// entry point): held here until the next call that may free them.
+static std::vector<IndexRef>& g_parked = *new std::vector<IndexRef>();
+
 // drop entries of the same buffer whose stream range overlaps [bit0, end);
-// their memory is released when the last holder lets go
-void registry_invalidate(const void* begin, uint64_t bit0, uint64_t end) {
+// their memory is released when the last holder lets go -- or, with `park`,
+// not before the next registry call without it
+static void drop_overlapping(const void* begin, uint64_t bit0, uint64_t end, bool park) {
   std::lock_guard<std::mutex> lk(g_reg_mu);
+  if (!park) g_parked.clear();
   for (size_t i = 0; i < g_reg.size();) {
     IndexEntry& e = g_reg[i];
-    if (e.begin == begin && e.bit0 < end && bit0 < e.end_bit) g_reg.erase(g_reg.begin() + i);
-    else i++;
+    if (e.begin == begin && e.bit0 < end && bit0 < e.end_bit) {
+      if (park) g_parked.push_back(std::move(e.index));
+      g_reg.erase(g_reg.begin() + i);
+    } else {
+      i++;
+    }
   }
+}
+
+void registry_invalidate(const void* begin, uint64_t bit0, uint64_t end) { drop_overlapping(begin, bit0, end, false); }
+
+void registry_invalidate_parked(const void* begin, uint64_t bit0, uint64_t end) {
+  drop_overlapping(begin, bit0, end, true);
 }
 
 void registry_insert(const IndexEntry& ne) {

@@ -89,6 +89,9 @@ struct IndexEntry {
 IndexEntry make_entry(const void* begin, uint64_t bit0, uint64_t end_bit, const FieldInfo& fi, const Job& j,
                       IndexRef index);
 void registry_invalidate(const void* begin, uint64_t bit0, uint64_t end);
+// the same without freeing anything now: dropped indexes are kept until the
+// next registry call that may free device memory
+void registry_invalidate_parked(const void* begin, uint64_t bit0, uint64_t end);
 void registry_insert(const IndexEntry& ne);
 bool registry_find(const void* begin, uint64_t bit0, const FieldInfo& fi, const zfp_stream* z, IndexEntry& out);
 

@@ -249,30 +249,6 @@ struct SmemSink {
   }
 };
 
-// Positional sink of emit_block_2p: ORs bits into the tile image at the
-// block's start + pos with 32-bit shared atomics (a block's first and last
-// words may hold a neighbour's bits).  `cap` counts logical 64-bit words;
-// bits past it are dropped and flagged.
-struct ImgOr {
-  uint64_t* buf;
-  uint32_t start;     // block's first bit in the image
-  uint32_t cap;
-  unsigned* status;
-  // one or two bits (v < 4): one 32-bit atomic, two when they straddle words
-  __device__ __forceinline__ void set_small(uint32_t pos, unsigned v, unsigned n) {
-    const uint32_t a = start + pos;
-    if (a + n > 64u * cap) {
-      atomicOr(status, (unsigned)kStatusOverflow);
-      return;
-    }
-    const uint32_t w = a >> 5;
-    const unsigned o = a & 31;
-    unsigned* b = (unsigned*)buf + w + ((w >> 5) << 1);   // 32-bit word w of the bank-spread image
-    atomicOr(b, v << o);
-    if (o + n > 32) atomicOr((unsigned*)buf + (w + 1) + (((w + 1) >> 5) << 1), v >> (32 - o));
-  }
-};
-
 // ---------------------------------------------------------------------------
 // CTA-wide exclusive scan of one value per thread
 
@@ -418,7 +394,7 @@ __device__ __forceinline__ void write_tile(const Job& job, const LaunchScratch& 
 template <typename S, int D, int kSel>
 __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch& sc, uint32_t gt, uint64_t* simg,
                                             uint32_t img_words, uint64_t* gslot, uint32_t slot_words,
-                                            uint64_t* planes) {
+                                            uint64_t* planes, const uint32_t* gtab) {
   using B = typename Traits<S>::Bits;
   using U = typename Traits<S>::UInt;
   constexpr int N = 1 << (2 * D);
@@ -464,9 +440,9 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
 
   if (active) {
     if constexpr (N <= 64) {
-      SmemSink seq{img, excl >> 6, excl & 63u, 0ull, true, nw, &job.result->status};
-      ImgOr pos{img, excl, nw, &job.result->status};
-      emit_block_2p<P, N>(seq, pos, h, my_planes, kTile);
+      SmemSink out{img, excl >> 6, excl & 63u, 0ull, true, nw, &job.result->status};
+      emit_block_seq<P, N>(out, h, my_planes, kTile, gtab);
+      out.finish();
     } else {
       SmemSink out{img, excl >> 6, excl & 63u, 0ull, true, nw, &job.result->status};
       wc.emit(out);
@@ -629,13 +605,15 @@ __device__ __forceinline__ void encode_body(const Job& one, const Job* jobs, int
   uint64_t* planes = plane_base<S, D, kMulti, kSel>(smem_img + img_words, one);
   __shared__ uint32_t s_tile;
   __shared__ Job s_job;
+  __shared__ uint32_t s_gtab[256];   // group-test codes of every byte (emit_block_seq)
+  for (uint32_t i = threadIdx.x; i < 256; i += kTile) s_gtab[i] = group_code_entry(i);
   for (uint32_t iter = blockIdx.x;; iter += gridDim.x) {
     if (threadIdx.x == 0) s_tile = use_ticket ? atomicAdd(sc.ticket, 1u) : iter;
     __syncthreads();
     const uint32_t gt = s_tile;
     if (gt >= total_tiles) break;
     const Job* job = resolve_job<kMulti>(one, jobs, njobs, gt, &s_job);
-    encode_tile<S, D, kSel>(*job, sc, gt, smem_img, img_words, gslot, slot_words, planes);
+    encode_tile<S, D, kSel>(*job, sc, gt, smem_img, img_words, gslot, slot_words, planes, s_gtab);
     __syncthreads();
   }
 }

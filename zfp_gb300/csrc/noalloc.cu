@@ -18,6 +18,7 @@
 // CUDA streams, or different host threads) race on it and must be ordered
 // by the caller.  Every GPU that loads the library holds the array until
 // the process exits.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -37,23 +38,52 @@ static_assert(64 + ((size_t)kNoAllocMaxTiles + 1) * 28 <= kNoAllocBytes, "scratc
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 static std::mutex g_noalloc_mu;
-static void* g_noalloc_addr[256];  // per device ordinal, resolved on the first call on that device
 
-// Device address of g_noalloc_scratch on the current device.  In host code
+// Set-up, per device: the device address of g_noalloc_scratch.  In host code
 // the array's name is only a host-side handle, so the address is looked up
-// once per device with cudaGetSymbolAddress while that device is current.
+// with cudaGetSymbolAddress while that device is current.  It is kept with
+// the driver context it was looked up in: after cudaDeviceReset the device's
+// next context loads the module again, possibly elsewhere, and the lookup
+// is repeated.
+struct ScratchAddr {
+  void* ctx = nullptr;
+  void* addr = nullptr;
+};
+static ScratchAddr g_noalloc_addr[256];   // per device ordinal
+
+static void* current_context() {
+  using GetCtx = CUresult (*)(CUcontext*);
+  static GetCtx get_ctx = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      fn = nullptr;
+    }
+    return (GetCtx)fn;
+  }();
+  CUcontext c = nullptr;
+  return get_ctx && get_ctx(&c) == CUDA_SUCCESS ? (void*)c : nullptr;
+}
+
 static void* noalloc_scratch(cudaError_t& err) {
   int dev = 0;
   err = cudaGetDevice(&dev);
   if (err != cudaSuccess || dev < 0 || dev >= 256) return nullptr;
+  // the caller has already made runtime calls on this device (pointer
+  // queries), so its primary context is current on this thread
+  void* ctx = current_context();
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_addr[dev]) {
+  ScratchAddr& s = g_noalloc_addr[dev];
+  if (!s.addr || !ctx || s.ctx != ctx) {
     void* p = nullptr;
     err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (err != cudaSuccess) return nullptr;
-    g_noalloc_addr[dev] = p;
+    s.addr = p;
+    s.ctx = ctx ? ctx : current_context();
   }
-  return g_noalloc_addr[dev];
+  return s.addr;
 }
 
 }  // namespace zg
@@ -121,6 +151,9 @@ extern "C" size_t zfp_gb300_compress_noalloc(zfp_stream* z, const zfp_field* f) 
   if (res.status)
     return fail(res.status & kStatusOverflow ? "zfp_gb300_compress_noalloc: stream buffer too small"
                                              : "zfp_gb300_compress_noalloc: GPU wait timed out");
+  // a block index kept for an earlier stream at the same place no longer
+  // describes it; the dropped index is freed by a later call, not this one
+  registry_invalidate_parked(ss.begin, bit0, res.end_bit);
   set_stream_flushed(z->stream, res.end_bit);
   set_error("");
   return (size_t)((res.end_bit + 63) / 64) * 8;
