@@ -10,8 +10,11 @@ device-resident, through the C ABI (zfp_compress / zfp_decompress,
 zfp_exec_cuda).  value = raw bytes coded per second (both directions).
 e2e = the same sweep with host (pinned) field and stream buffers, so the
 host<->device copies are inside the timed region.  `--impl reference` times
-the reference's CPU algorithm (the oracle port: OpenMP compress, serial
-decompress -- the reference has no OpenMP decompressor) on a bounded sample.
+the reference's own CPU codec (its library compiled from its sources:
+OpenMP compress on all host cores, serial decompress -- the reference has
+no OpenMP decompressor -- plus serial compress on one core) on a bounded
+sample; `reference_cuda` times the reference's own CUDA backend on the same
+fields at fixed rate 8 beside this library's kernels.
 """
 from __future__ import annotations
 
@@ -50,6 +53,7 @@ def parse_args():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-batch", action="store_true")
     p.add_argument("--no-serve", action="store_true")
+    p.add_argument("--no-refcuda", action="store_true")
     p.add_argument("--only", default=None,
                    help="profiling: run one kernel, FIELD:MODE:DIR (e.g. f32:rate:c), --steps times")
     p.add_argument("--shape", default=None, help="profiling: field shape Z,Y,X for --only")
@@ -308,6 +312,11 @@ def gpu_arm(args):
                 "traffic": traffic.get(key)}
     fixed = [r for r in per if r["mode"] == "rate"]
 
+    # the reference's own CUDA backend on the same fields (fixed rate 8)
+    ref_cuda = None
+    if not args.no_refcuda:
+        ref_cuda = reference_cuda_column(fields, one, torch, reps)
+
     # end to end: host pinned buffers through the same C API (synchronous calls)
     ratios = {f"{fd['name']}_{m}": round(fd["raw"] / fd["sizes"][m], 3) for fd in fields for m, _ in MODES}
     shapes = [list(fd["shape"]) for fd in fields]
@@ -345,6 +354,7 @@ def gpu_arm(args):
             "fixed_rate": {f"{r['field']}_{r['dir']}": {"raw_gbs": round(r["raw_gbs"], 1),
                                                          "hbm_frac": round(r["hbm_gbs"] / peak, 4)} for r in fixed},
             "per_kernel": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in r.items()} for r in per],
+            "reference_cuda": ref_cuda,
             "checks": checks,
             "compression_ratio": ratios,
             "batch": batch,
@@ -723,21 +733,93 @@ def e2e_run(lib, torch, codec, fields, args):
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline: the oracle port of the reference's CPU path
+# CPU baseline: the reference's own CPU codec (the library compiled from its
+# sources by oracle/Makefile), driven through its public C API; the oracle
+# port of it only where the reference could not be compiled
+
+REF_CPU_LIB = os.path.join(ROOT, "oracle", "_ref", "libzfp_ref.so")
+REF_CUDA_LIB = os.path.join(ROOT, "baseline", "_ref", "libzfp_refcuda.so")
+CPU_SAMPLE_PLANES = {"f32": 16, "f64": 12}
+
 
 def cpu_sample(fields_spec, small):
-    """A bounded sample of each field: the first z-planes (same generator)."""
+    """A bounded sample of each field: its first z-planes (same generator, same seed)."""
     from zfp_gb300 import synth
     out = []
     for name, shape, seed in fields_spec:
         dt = np.float32 if name == "f32" else np.float64
-        planes = max(4, min(shape[0], (48 if name == "f32" else 32) if not small else 8))
+        planes = min(shape[0], CPU_SAMPLE_PLANES[name] if not small else 8)
         sub = (planes, shape[1], shape[2])
         out.append((name, sub, synth.smooth_field(sub, dt, seed=seed, noise=1e-2)))
     return out
 
 
-def cpu_measure(samples, threads, reps=1):
+def ref_cpu_lib():
+    """The reference library, built from its own sources (None if it could not be built here)."""
+    if not os.path.exists(REF_CPU_LIB):
+        return None
+    from zfp_gb300 import capi
+    return capi.ZfpLib(REF_CPU_LIB)
+
+
+def ref_cpu_measure(lib, samples, threads, reps=1):
+    """Per mode and sample field, through the reference's zfp_compress /
+    zfp_decompress: serial compress (1 core), OpenMP compress (`threads`
+    cores; its stream must equal the serial one) and serial decompress (the
+    reference has no OpenMP decompressor, src/zfp.c:1137-1138).  Returns raw
+    bytes per direction and the three times in seconds."""
+    from zfp_gb300 import capi
+    raw = 0
+    t_ser = t_omp = t_dec = 0.0
+    for _ in range(reps):
+        for name, sub, a in samples:
+            ztype = capi.TYPE_FLOAT if a.dtype == np.float32 else capi.TYPE_DOUBLE
+            n = tuple(reversed(a.shape))
+            for mode, arg in MODES:
+                z = lib.zfp_stream_open(None)
+                capi.set_mode(lib, z, mode, arg, ztype, 3)
+                f = capi.make_field(lib, a.ctypes.data, ztype, n)
+                cap = lib.zfp_stream_maximum_size(z, f)
+                streams = []
+                for policy in (capi.EXEC_SERIAL, capi.EXEC_OMP):
+                    buf = np.zeros(cap // 8 + 1, dtype=np.uint64)
+                    bs = lib.stream_open(buf.ctypes.data, buf.nbytes)
+                    lib.zfp_stream_set_bit_stream(z, bs)
+                    if policy == capi.EXEC_OMP:
+                        assert lib.zfp_stream_set_omp_threads(z, threads)
+                    else:
+                        assert lib.zfp_stream_set_execution(z, capi.EXEC_SERIAL)
+                    lib.zfp_stream_rewind(z)
+                    t0 = time.perf_counter()
+                    size = lib.zfp_compress(z, f)
+                    dt = time.perf_counter() - t0
+                    assert size, f"reference compress failed ({name} {mode})"
+                    if policy == capi.EXEC_OMP:
+                        t_omp += dt
+                    else:
+                        t_ser += dt
+                    streams.append((buf, size, bs))
+                (b0, s0, bs0), (b1, s1, bs1) = streams
+                assert s0 == s1 and np.array_equal(b0[: s0 // 8], b1[: s1 // 8]), "OpenMP stream differs from serial"
+                out = np.empty_like(a)
+                lib.zfp_field_set_pointer(f, out.ctypes.data)
+                assert lib.zfp_stream_set_execution(z, capi.EXEC_SERIAL)
+                lib.zfp_stream_set_bit_stream(z, bs0)
+                lib.zfp_stream_rewind(z)
+                t0 = time.perf_counter()
+                assert lib.zfp_decompress(z, f) == s0
+                t_dec += time.perf_counter() - t0
+                raw += a.nbytes
+                lib.zfp_field_free(f)
+                lib.zfp_stream_close(z)
+                lib.stream_close(bs0)
+                lib.stream_close(bs1)
+    return raw, t_ser, t_omp, t_dec
+
+
+def port_measure(samples, threads, reps=1):
+    """The oracle port (a C restatement of the reference's serial codec), only
+    where the reference itself could not be compiled."""
     from oracle.pyoracle import Oracle, mode_params
     orc = Oracle()
     raw = 0
@@ -754,44 +836,136 @@ def cpu_measure(samples, threads, reps=1):
                 t2 = time.perf_counter()
                 t_c += t1 - t0
                 t_d += t2 - t1
-                raw += 2 * a.nbytes
+                raw += a.nbytes
     return raw, t_c, t_d
+
+
+def sample_text(samples):
+    return ", ".join(f"{n} {list(s)}" for n, s, _ in samples)
+
+
+def cpu_columns(samples, threads, reps, warm=True):
+    """The baseline's value (GB/s of raw bytes, compress + decompress, each
+    direction on the reference's fastest CPU path: OpenMP compress, serial
+    decompress) and its columns."""
+    lib = ref_cpu_lib()
+    if lib is not None:
+        if warm:
+            ref_cpu_measure(lib, samples, threads)
+        raw, t_ser, t_omp, t_dec = ref_cpu_measure(lib, samples, threads, reps)
+        return {"value": round(2 * raw / (t_omp + t_dec) / 1e9, 4), "unit": "GB/s", "cores": threads,
+                "kind": "reference",
+                "sample": "the reference library (its own sources, compiled by oracle/Makefile) through "
+                          "zfp_compress / zfp_decompress, 4 modes, over the first z-planes of each field: "
+                          + sample_text(samples),
+                "serial_compress_gbs_1core": round(raw / t_ser / 1e9, 4),
+                "omp_compress_gbs": round(raw / t_omp / 1e9, 4), "omp_threads": threads,
+                "serial_decompress_gbs_1core": round(raw / t_dec / 1e9, 4),
+                "omp_decompress": "none in the reference (src/zfp.c:1137-1138)"}, (t_omp + t_dec)
+    if warm:
+        port_measure(samples, threads)
+    raw, t_c, t_d = port_measure(samples, threads, reps)
+    return {"value": round(2 * raw / (t_c + t_d) / 1e9, 4), "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": "oracle port (the reference library could not be compiled here): OpenMP compress, serial "
+                      "decompress, over the first z-planes of each field: " + sample_text(samples),
+            "compress_gbs": round(raw / t_c / 1e9, 4), "decompress_gbs": round(raw / t_d / 1e9, 4)}, (t_c + t_d)
 
 
 def cpu_baseline(fields, args):
     spec = [(fd["name"], fd["shape"], 1) for fd in fields]
     samples = cpu_sample(spec, args.small)
     threads = os.cpu_count() or 1
-    raw, t_c, t_d = cpu_measure(samples, threads)
-    return {"value": round(raw / (t_c + t_d) / 1e9, 4), "unit": "GB/s", "cores": threads, "kind": "port",
-            "sample": "oracle (C restatement of the reference's serial codec): OpenMP compress on all cores, "
-                      "serial decompress, over the first z-planes of each field: "
-                      + ", ".join(f"{n} {list(s)}" for n, s, _ in samples),
-            "compress_gbs": round(raw / 2 / t_c / 1e9, 4), "decompress_gbs": round(raw / 2 / t_d / 1e9, 4)}
+    cols, _ = cpu_columns(samples, threads, reps=12 if not args.small else 1)
+    return cols
 
 
 def reference_arm(args):
+    """The reference's own CPU implementation of the path on this host's
+    cores, on the same fields and modes (a bounded sample per step)."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
-    from oracle import pyoracle
-    pyoracle.build()
     samples = cpu_sample(field_shapes(args.small), args.small)
     threads = os.cpu_count() or 1
-    cpu_measure(samples, threads)  # warm
     for _ in range(max(0, args.warmup - 1)):
-        cpu_measure(samples, threads)
-    raw, t_c, t_d = cpu_measure(samples, threads, reps=args.steps)
-    value = raw / (t_c + t_d) / 1e9
-    line = {"metric": METRIC, "value": round(value, 4), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round((t_c + t_d) * 1e3 / args.steps, 3),
+        cpu_columns(samples, threads, 1, warm=False)
+    cols, secs = cpu_columns(samples, threads, args.steps)
+    value = cols["value"]
+    line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(secs * 1e3 / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 in, u64 stream",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": "same fields and modes, bounded sample per step (first z-planes)"},
-            "cpu_baseline": {"value": round(value, 4), "unit": "GB/s", "cores": threads, "kind": "port",
-                             "sample": ", ".join(f"{n} {list(s)}" for n, s, _ in samples)},
-            "e2e": {"value": round(value, 4), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "config": {"workload": "same fields and modes, bounded sample per step (first z-planes): "
+                                   + sample_text(samples)},
+            "cpu_baseline": cols,
+            "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def reference_cuda_column(fields, codec_one, torch, reps):
+    """The reference's own CUDA backend (src/cuda_zfp, compiled for sm_103a by
+    oracle/Makefile into baseline/_ref) on the same fields at fixed rate 8,
+    the only mode and dimensionality range it supports (1-3D, fixed rate),
+    through zfp_compress / zfp_decompress with device-resident field and
+    stream, timed with CUDA events on the stream it uses (the legacy
+    default stream) like this library's kernels.  Its streams and decoded
+    arrays are checked against this library's."""
+    if not os.path.exists(REF_CUDA_LIB):
+        return {"unavailable": "the reference's CUDA backend was not built (no reference sources here)"}
+    from zfp_gb300 import capi
+    lib = capi.ZfpLib(REF_CUDA_LIB)
+    out = {}
+    legacy = torch.cuda.default_stream()
+    for fd in fields:
+        ztype, n = fd["ztype"], fd["n"]
+        z = lib.zfp_stream_open(None)
+        capi.set_mode(lib, z, "rate", 8.0, ztype, 3)
+        if not lib.zfp_stream_set_execution(z, capi.EXEC_CUDA):
+            return {"unavailable": "the reference library was built without its CUDA backend"}
+        f = capi.make_field(lib, fd["x"].data_ptr(), ztype, n)
+        cap = lib.zfp_stream_maximum_size(z, f)
+        buf = torch.zeros(cap // 8 + 8, dtype=torch.int64, device="cuda")
+        bs = lib.stream_open(buf.data_ptr(), buf.numel() * 8)
+        lib.zfp_stream_set_bit_stream(z, bs)
+        size = lib.zfp_compress(z, f)
+        torch.cuda.synchronize()
+        mine = codec_one(fd, "rate", 8.0, "c")
+        torch.cuda.synchronize()
+        same_stream = size == mine and torch.equal(buf[: size // 8], fd["bufs"]["rate"][: size // 8])
+        # decode both streams; the arrays must agree
+        codec_one(fd, "rate", 8.0, "d")
+        torch.cuda.synchronize()
+        my_out = fd["out"].clone()
+        rout = torch.empty_like(fd["x"])
+        fo = capi.make_field(lib, rout.data_ptr(), ztype, n)
+        lib.zfp_stream_rewind(z)
+        dsize = lib.zfp_decompress(z, fo)
+        torch.cuda.synchronize()
+        bits = torch.int32 if fd["name"] == "f32" else torch.int64
+        same_out = dsize == size and torch.equal(rout.view(bits), my_out.view(bits))
+        res = {"stream_bytes": int(size), "stream_equal": bool(same_stream), "decoded_equal": bool(same_out)}
+        for direction, fld in (("compress", f), ("decompress", fo)):
+            fn = lib.zfp_compress if direction == "compress" else lib.zfp_decompress
+            for _ in range(2):
+                lib.zfp_stream_rewind(z)
+                fn(z, fld)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(legacy)
+            for _ in range(reps):
+                lib.zfp_stream_rewind(z)
+                fn(z, fld)
+            e1.record(legacy)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            res[direction] = {"ms": round(ms, 4), "raw_gbs": round(fd["raw"] / ms / 1e6, 1),
+                              "hbm_gbs": round((fd["raw"] + size) / ms / 1e6, 1)}
+        lib.zfp_field_free(f)
+        lib.zfp_field_free(fo)
+        lib.zfp_stream_close(z)
+        lib.stream_close(bs)
+        out[f"{fd['name']}_rate8"] = res
+    return out
 
 
 def profile_one(args):

@@ -41,7 +41,7 @@ def build(quiet: bool = True) -> str:
     return LIB_PATH
 
 
-REF_CUDA_LIB_PATH = os.path.join(HERE, "_ref", "libzfp_refcuda.so")
+REF_CUDA_LIB_PATH = os.path.join(os.path.dirname(HERE), "baseline", "_ref", "libzfp_refcuda.so")
 STAGED = os.path.join(HERE, "_ref", "src")
 
 
@@ -92,7 +92,9 @@ def build_ref(quiet: bool = True) -> str | None:
 
 
 def build_ref_cuda(quiet: bool = True) -> str | None:
-    """Compile the reference library with its own CUDA backend (src/cuda_zfp) for sm_103a."""
+    """Compile the reference library with its own CUDA backend (src/cuda_zfp) for
+    sm_103a into baseline/_ref: the benchmark's comparison column (it is not
+    part of the checker)."""
     return _make("refcuda", REF_CUDA_LIB_PATH, quiet)
 
 
