@@ -383,20 +383,10 @@ def batch_compare(lib, torch, stream, args):
     (seed 2), amplitude scale 10^U(-3,3); half fixed-rate (rate in
     {4,8,12,16,24,32}), half fixed-accuracy (tolerance 10^U(-5,-2)).  One
     batched launch against one zfp_compress / zfp_decompress per array."""
-    from zfp_gb300 import capi, synth
+    from zfp_gb300 import capi, workloads
     L = bind_batch(lib)
-    rng = np.random.default_rng(2)
     count = 4096 if not args.small else 256
-    arrays = []
-    for i in range(count):
-        shape = tuple(int(v) for v in np.exp(rng.uniform(np.log(8), np.log(128), size=3)).astype(int))
-        scale = float(10.0 ** rng.uniform(-3, 3))
-        x = synth.smooth_field_torch(shape, torch.float32, seed=int(rng.integers(1 << 31)), noise=1e-2, scale=scale)
-        if i % 2 == 0:
-            mode, arg = "rate", float(rng.choice([4, 8, 12, 16, 24, 32]))
-        else:
-            mode, arg = "accuracy", float(10.0 ** rng.uniform(-5, -2))
-        arrays.append((x, mode, arg))
+    arrays = workloads.batch_arrays(torch, count)
     raw = sum(x.numel() * 4 for x, _, _ in arrays)
 
     def objects(outs, bufs, use_out):
@@ -488,7 +478,7 @@ def serve_compare(lib, torch, args):
     requests read streams compressed before the timed run."""
     import queue
 
-    from zfp_gb300 import capi, synth
+    from zfp_gb300 import capi, workloads
     L = lib.lib
     L.zfp_gb300_server_create.restype = C.c_void_p
     L.zfp_gb300_server_create.argtypes = [C.c_size_t, C.c_int]
@@ -497,37 +487,12 @@ def serve_compare(lib, torch, args):
     L.zfp_gb300_server_wait.restype = C.c_size_t
     L.zfp_gb300_server_wait.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(C.c_double)]
     L.zfp_gb300_server_free.argtypes = [C.c_void_p]
-    rng = np.random.default_rng(3)
     count = 20000 if not args.small else 600
     smax = (256 << 20) if not args.small else (8 << 20)
     rate = 6000.0 if not args.small else 2000.0
-    bases = {}
-    for dt, esz in ((torch.float32, 4), (torch.float64, 8)):
-        for dims in (2, 3):
-            side = int((smax / esz) ** (1.0 / dims)) + 1
-            bases[(esz, dims)] = synth.smooth_field_torch((side,) * dims, dt, seed=3 + esz + dims, noise=1e-2)
-    def random_field():
-        esz = 4 if rng.random() < 0.5 else 8
-        dims = 2 if rng.random() < 0.5 else 3
-        size = float(np.exp(rng.uniform(np.log(16 << 10), np.log(smax))))
-        base = bases[(esz, dims)]
-        n = max(4, min(base.shape[0], int(round((size / esz) ** (1.0 / dims)))))
-        view = base[(slice(0, n),) * dims]
-        lo, hi = torch.aminmax(view)
-        return dict(view=view, esz=esz, dims=dims, tol=1e-4 * float(hi - lo), raw=view.numel() * esz)
-
-    # decompress requests draw from 64 templates (same size distribution), each compressed once
-    templates = [random_field() for _ in range(64)]
-    reqs = []
-    for i in range(count):
-        if rng.random() < 0.7:
-            reqs.append(dict(random_field(), direction=0))
-        else:
-            t = int(rng.integers(len(templates)))
-            reqs.append(dict(templates[t], direction=1, template=t))
+    mix = workloads.ServingMix(torch, count, smax=smax, rate=rate)
+    bases, templates, reqs, arrivals = mix.bases, mix.templates, mix.requests, mix.arrivals
     total_raw = sum(r["raw"] for r in reqs)
-    gaps = rng.exponential(1.0 / rate, size=count)
-    arrivals = np.cumsum(gaps) - gaps[0]
 
     def make_objects(r, buf_ptr, nbytes, out_ptr=None):
         bs = lib.stream_open(buf_ptr, nbytes)

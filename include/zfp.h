@@ -21,12 +21,8 @@
 #include <stdint.h>
 
 #include "bitstream.h"
-
-/* versions (reference include/zfp/version.h:5-14): codec 5, library 1.0.1 */
-#define ZFP_VERSION_MAJOR 1
-#define ZFP_VERSION_MINOR 0
-#define ZFP_VERSION_PATCH 1
-#define ZFP_CODEC 5
+#include "zfp/version.h"              /* versions (reference include/zfp/version.h): codec 5, library 1.0.1 */
+#include "zfp/internal/zfp/types.h"   /* int32, uint, ... (reference include/zfp.h:13) */
 
 /* default compression parameters (include/zfp.h:18-21) */
 #define ZFP_MIN_BITS 1

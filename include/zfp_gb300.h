@@ -40,6 +40,23 @@ const char* zfp_gb300_last_error(void);
  * host buffers are staged through device memory. */
 size_t zfp_gb300_last_staged_bytes(void);
 
+/* ---- failure detection ---------------------------------------------------
+ * No counterpart in the reference (its encoders never wait on each other).
+ * A variable-rate encoder tile waits, on the GPU, for the bit counts of the
+ * tiles before it.  Every such wait is bounded: past this many SM clock
+ * cycles the tile takes its predecessor to be lost, the call returns 0 with
+ * "GPU wait timed out" in zfp_gb300_last_error(), and the CUDA context stays
+ * usable.  0 selects the default, 4e9 cycles (about 2 s at GB300 clocks).
+ * Applies to launches made after the call, in this process; returns the
+ * previous setting. */
+unsigned long long zfp_gb300_set_wait_limit(unsigned long long cycles);
+
+/* Test hook for the bounded wait above, acting on the host: when enabled,
+ * the next variable-rate zfp_compress hands out its tiles from the second
+ * one on, so the second tile waits for a predecessor that never runs.  That
+ * call fails as described above and clears the hook. */
+void zfp_gb300_test_skip_first_tile(int enable);
+
 /* ---- batches: many fields in one launch --------------------------------
  * A batch codes `count` independent fields, each with its own zfp_stream
  * (mode, parameters and bit stream, positioned where that stream's next

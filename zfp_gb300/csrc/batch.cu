@@ -250,6 +250,7 @@ zfp_gb300_batch* zfp_gb300_batch_create(zfp_stream* const* streams, const zfp_fi
     g.sc.tile_state = (unsigned long long*)(p + 64);
     g.sc.side = (unsigned long long*)(p + 64 + t * 8);
     g.sc.side_cnt = (unsigned int*)(p + 64 + t * 24);
+    g.sc.wait_cycles = wait_cycles();
     LaunchArgs probe;
     std::memset(&probe, 0, sizeof probe);
     probe.jobs = g.d_jobs;

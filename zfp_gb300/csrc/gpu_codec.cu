@@ -23,6 +23,8 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
+#include <climits>
 #include <mutex>
 #include <string>
 #include <type_traits>
@@ -432,6 +434,14 @@ cudaError_t launch_parse_any(int type, int dims, const Job& j, cudaStream_t st) 
   return by_type(type, dims, [&](auto s, auto d) { return run_parse<decltype(s), decltype(d)::value>(j, st); });
 }
 
+// bound on the encoder's look-back waits (0: the kernels' default), and the
+// failure-detection test hook: the next variable-rate zfp_compress skips its
+// first tile
+static std::atomic<long long> g_wait_cycles{0};
+static std::atomic<int> g_skip_first_tile{0};
+
+long long wait_cycles() { return g_wait_cycles.load(std::memory_order_relaxed); }
+
 // scratch for one launch: result slot + look-back / boundary state, zeroed
 struct LaunchMem {
   DevBuf buf;
@@ -448,6 +458,7 @@ struct LaunchMem {
     sc.tile_state = (unsigned long long*)(p + 64);
     sc.side = (unsigned long long*)(p + 64 + t * 8);
     sc.side_cnt = (unsigned int*)(p + 64 + t * 24);
+    sc.wait_cycles = wait_cycles();
     return cudaMemsetAsync(p, 0, bytes, st);
   }
 };
@@ -523,6 +534,10 @@ size_t gpu_compress(zfp_stream* z, const zfp_field* f) {
   LaunchMem lm;
   if ((e = lm.make(job.ntiles, st)) != cudaSuccess) return fail_cuda("zfp_compress: scratch", e);
   job.result = lm.result;
+  // test hook: hand tiles out from the second one, so that the second
+  // tile's look-back waits for a tile that never runs
+  if (!fixed && g_skip_first_tile.exchange(0) && (e = cudaMemsetAsync(lm.sc.ticket, 1, 1, st)) != cudaSuccess)
+    return fail_cuda("zfp_compress: scratch", e);
 
   LaunchArgs a;
   std::memset(&a, 0, sizeof a);
@@ -770,3 +785,10 @@ const char* zfp_gb300_last_error(void) { return zg::g_last_error.c_str(); }
 size_t zfp_gb300_last_staged_bytes(void) { return zg::g_staged; }
 
 }  // extern "C"
+
+extern "C" unsigned long long zfp_gb300_set_wait_limit(unsigned long long cycles) {
+  const long long v = cycles > (unsigned long long)LLONG_MAX ? LLONG_MAX : (long long)cycles;
+  return (unsigned long long)zg::g_wait_cycles.exchange(v);
+}
+
+extern "C" void zfp_gb300_test_skip_first_tile(int enable) { zg::g_skip_first_tile.store(enable ? 1 : 0); }

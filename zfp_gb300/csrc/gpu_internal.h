@@ -42,6 +42,8 @@ Job base_job(const FieldInfo& fi, const zfp_stream* z, void* field);
 int persistent_grid();
 
 bool is_device_ptr(const void* p);
+// the look-back wait bound every launch uses (zfp_gb300_set_wait_limit; 0: default)
+long long wait_cycles();
 void init_pool_once();
 size_t fail(const char* msg);
 size_t fail_cuda(const char* where, cudaError_t e);

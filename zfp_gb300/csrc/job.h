@@ -59,7 +59,12 @@ struct LaunchScratch {
   unsigned long long* side;        // per tile boundary: tail part, head part
   unsigned int* side_cnt;          // per tile boundary: arrivals
   unsigned int* ticket;            // next tile to hand out
+  long long wait_cycles;           // bound on each look-back wait, in SM clock cycles (0: kDefaultWaitCycles)
 };
+
+// ~2 s at GB300 clocks: a predecessor tile that has not published its bit
+// count by then is taken to be lost, and the launch fails instead of hanging
+constexpr long long kDefaultWaitCycles = 4000000000ll;
 
 inline size_t scratch_bytes(uint32_t total_tiles) {
   const size_t t = (size_t)total_tiles + 1;

@@ -279,7 +279,6 @@ __device__ __forceinline__ uint32_t cta_exclusive_scan(uint32_t v, uint32_t& tot
 constexpr unsigned long long kStateAgg = 1ull << 62;
 constexpr unsigned long long kStateIncl = 2ull << 62;
 constexpr unsigned long long kStateValue = (1ull << 62) - 1;
-constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at GB300 clocks: then give up
 
 __device__ __forceinline__ void publish_state(unsigned long long* slot, unsigned long long v) {
   __threadfence();
@@ -302,6 +301,7 @@ __device__ __forceinline__ uint64_t look_back(const Job& job, const LaunchScratc
   uint64_t exclusive = 0;
   int64_t pred = (int64_t)gt - 1 - lane;
   const long long t0 = clock64();
+  const long long wait_limit = sc.wait_cycles > 0 ? sc.wait_cycles : kDefaultWaitCycles;
   bool timed_out = false;
   for (;;) {
     unsigned long long st = kStateIncl;  // before the job's first tile: inclusive 0
@@ -309,7 +309,7 @@ __device__ __forceinline__ uint64_t look_back(const Job& job, const LaunchScratc
       const volatile unsigned long long* slot = sc.tile_state + pred;
       st = *slot;
       while (!(st >> 62)) {
-        if (clock64() - t0 > kWaitCycles) {
+        if (clock64() - t0 > wait_limit) {
           timed_out = true;
           st = kStateIncl;
           break;

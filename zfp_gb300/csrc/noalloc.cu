@@ -137,6 +137,7 @@ extern "C" size_t zfp_gb300_compress_noalloc(zfp_stream* z, const zfp_field* f) 
   a.sc.tile_state = (unsigned long long*)(scratch + 64);
   a.sc.side = (unsigned long long*)(scratch + 64 + t * 8);
   a.sc.side_cnt = (unsigned int*)(scratch + 64 + t * 24);
+  a.sc.wait_cycles = wait_cycles();
   a.total_tiles = (uint32_t)ntiles;
   a.use_ticket = fixed ? 0 : 1;
   a.img_words = (uint32_t)img_words;

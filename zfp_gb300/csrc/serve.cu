@@ -182,6 +182,7 @@ static cudaError_t launch_batch(Server* s, Lane* lane) {
     a.sc.tile_state = (unsigned long long*)(p + 64);
     a.sc.side = (unsigned long long*)(p + 64 + t * 8);
     a.sc.side_cnt = (unsigned int*)(p + 64 + t * 24);
+    a.sc.wait_cycles = wait_cycles();
     a.total_tiles = g.tiles;
     a.use_ticket = 1;
     // encode keeps whole tile images in shared memory (no global slots);
