@@ -91,13 +91,19 @@ zfp_bool zfp_gb300_batch_set_ctas_per_sm(zfp_gb300_batch* batch, int ctas_per_sm
 /* ---- serving: continuous batching of independent requests --------------
  * A server runs compress / decompress requests on device-resident fields
  * and streams as they arrive.  A dispatcher thread keeps `lanes` CUDA
- * streams busy: whenever a lane is free it admits waiting requests in
- * arrival order while the bytes of all admitted, unfinished requests (field
- * span plus stream capacity) stay within `hbm_budget`, and launches them as
- * one batch (one persistent launch per scalar type and dimensionality).
- * Requests that arrive while batches run join the next batch on the next
- * free lane, so work from different batches overlaps on the GPU.  Results
- * are the same streams/arrays zfp_compress / zfp_decompress produce. */
+ * streams busy.  Requests are sorted by the raw size of their field into
+ * classes (up to 2 MiB, up to 32 MiB, larger), each with its own queue; the
+ * first lanes serve one class each (small, medium, large), the others the
+ * large class, and a class without a lane of its own is served by the
+ * largest class that has one.  Whenever a lane is free it admits waiting
+ * requests of its class in arrival order while the bytes of all admitted,
+ * unfinished requests (field span plus stream capacity) stay within
+ * `hbm_budget`, and launches them as one batch (one persistent launch per
+ * scalar type and dimensionality); a request completes with its batch, so
+ * small requests never wait for large ones.  Requests that arrive while
+ * batches run join the next batch on the next free lane of their class, so
+ * work from different batches overlaps on the GPU.  Results are the same
+ * streams/arrays zfp_compress / zfp_decompress produce. */
 typedef struct zfp_gb300_server zfp_gb300_server;
 
 zfp_gb300_server* zfp_gb300_server_create(size_t hbm_budget, int lanes);
@@ -114,6 +120,11 @@ uint64_t zfp_gb300_server_submit(zfp_gb300_server* server, zfp_stream* zfp, cons
  * If seconds is not NULL it receives the time from submission to the end of
  * the request's GPU work. */
 size_t zfp_gb300_server_wait(zfp_gb300_server* server, uint64_t ticket, double* seconds);
+
+/* Counters since the server was created: the most bytes ever admitted at
+ * once (never above the budget), batches launched, requests completed.
+ * Any pointer may be NULL.  Returns 0 for a NULL server. */
+int zfp_gb300_server_stats(zfp_gb300_server* server, size_t* peak_bytes, uint64_t* batches, uint64_t* served);
 
 /* Finish everything submitted, stop the dispatcher and release the server. */
 void zfp_gb300_server_free(zfp_gb300_server* server);

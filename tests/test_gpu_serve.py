@@ -25,6 +25,9 @@ def bind(lib):
     L.zfp_gb300_server_wait.restype = C.c_size_t
     L.zfp_gb300_server_wait.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(C.c_double)]
     L.zfp_gb300_server_free.argtypes = [C.c_void_p]
+    L.zfp_gb300_server_stats.restype = C.c_int
+    L.zfp_gb300_server_stats.argtypes = [C.c_void_p, C.POINTER(C.c_size_t), C.POINTER(C.c_uint64),
+                                         C.POINTER(C.c_uint64)]
     return L
 
 
@@ -128,6 +131,13 @@ def test_server_results_equal_alone(lib, cuda):
         assert torch.equal(reqs[i].out.view(torch.int8), alone_out[i].view(torch.int8))
     for r in reqs:
         r.close()
+    # the budget was honoured: admitted bytes never exceeded it, and it did
+    # bind (more than one batch was needed for what was queued)
+    peak, batches, served = C.c_size_t(), C.c_uint64(), C.c_uint64()
+    assert L.zfp_gb300_server_stats(server, C.byref(peak), C.byref(batches), C.byref(served))
+    assert 0 < peak.value <= (64 << 20)
+    assert served.value == len(reqs) + len(tickets)
+    assert batches.value > 1
     L.zfp_gb300_server_free(server)
 
 

@@ -2,14 +2,17 @@
 //
 // The reference serves nothing; a caller of zfp_compress waits for each
 // field in turn.  Here a dispatcher thread owns a few CUDA streams ("lanes").
-// Submissions go into a FIFO.  Whenever a lane is free the dispatcher takes
-// requests from the front of the FIFO while the bytes held by admitted,
-// unfinished requests stay within the HBM budget, and launches them as one
-// batch: jobs grouped by (direction, type, dims), one persistent multi-job
-// launch per group (the same kernels as zfp_compress).  A host callback at the end of
-// the lane's work marks the batch complete and wakes the dispatcher, which
-// publishes the results, returns the budget and admits whatever arrived in
-// the meantime -- new work starts while other lanes are still running.
+// Requests are sorted by raw size into classes (up to 2 MiB, up to 32 MiB,
+// larger), each with its own FIFO and its own lanes, so a small request
+// never shares a launch with -- and never completes with -- a large one.
+// Whenever a lane is free the dispatcher takes requests from the front of
+// its class's FIFO while the bytes held by all admitted, unfinished requests
+// stay within the HBM budget, and launches them as one batch: jobs grouped
+// by (direction, type, dims), one persistent multi-job launch per group (the
+// same kernels as zfp_compress).  A host callback at the end of the lane's
+// work marks the batch complete and wakes the dispatcher, which publishes
+// the results, returns the budget and admits whatever arrived in the
+// meantime -- new work starts while other lanes are still running.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -41,6 +44,7 @@ struct Request {
   FieldInfo fi;
   Job job;
   size_t cost = 0;               // bytes counted against the budget
+  int cls = 0;                   // size class (of the lanes that serve it)
   bool fixed = false;
   uint64_t nominal_end = 0;
   IndexRef held;                 // decompress: the block index read (kept until the request is gone)
@@ -49,7 +53,18 @@ struct Request {
   size_t size = 0;
 };
 
+// request size classes: raw bytes up to these bounds, then the rest
+constexpr size_t kClassBound[] = {size_t(2) << 20, size_t(32) << 20};
+constexpr int kClasses = 3;
+
+static int size_class(size_t raw) {
+  int c = 0;
+  while (c < kClasses - 1 && raw > kClassBound[c]) c++;
+  return c;
+}
+
 struct Lane {
+  int cls = 0;                   // the size class it serves
   cudaStream_t st = nullptr;
   bool busy = false;
   std::atomic<bool> finished{false};
@@ -67,8 +82,11 @@ struct Lane {
 
 struct Server {
   size_t budget = 0, used = 0;
+  size_t peak = 0;               // most bytes ever admitted at once
+  uint64_t batches = 0, served = 0;
   std::vector<std::unique_ptr<Lane>> lanes;
-  std::deque<std::shared_ptr<Request>> pending;
+  std::deque<std::shared_ptr<Request>> pending[kClasses];   // per size class (lanes serve the classes they map to)
+  int lane_class_max = 0;
   std::unordered_map<uint64_t, std::shared_ptr<Request>> live;
   std::mutex mu;
   std::condition_variable cv;
@@ -118,7 +136,7 @@ static cudaError_t launch_batch(Server* s, Lane* lane) {
   // device layout: results | per group: jobs, scratch | block indexes
   size_t off = ((reqs.size() * sizeof(JobResult)) + 255) & ~(size_t)255;
   struct G { int type, dims; std::vector<size_t> idx; uint32_t tiles = 0, img_words = 0; size_t jobs_off, scr_off,
-             scr_bytes; };
+             scr_bytes; LaunchArgs one; size_t gimg_off = 0, gimg_bytes = 0; };
   std::vector<G> gs;
   for (auto& kv : groups) {
     G g;
@@ -138,6 +156,32 @@ static cudaError_t launch_batch(Server* s, Lane* lane) {
     g.scr_off = off;
     g.scr_bytes = 64 + t * 28;
     off += (g.scr_bytes + 255) & ~(size_t)255;
+    // a request alone in its group runs the kernel zfp_compress /
+    // zfp_decompress would pick for it (specialised to its mode and sized
+    // to it), planned the same way; several share the multi-job kernel
+    std::memset(&g.one, 0, sizeof g.one);
+    if (g.idx.size() == 1) {
+      const Request& r = *reqs[g.idx[0]];
+      LaunchArgs& a = g.one;
+      a.one = r.job;
+      a.njobs = 1;
+      a.total_tiles = g.tiles;
+      a.grid = (int)g.tiles;
+      a.use_ticket = r.direction == 0 && !r.fixed;
+      if (r.direction == 1 && g.tiles) {
+        const uint64_t end = r.fixed ? r.nominal_end : r.job.end_bit;
+        a.want_words = (uint32_t)std::min<uint64_t>(image_words((end - r.job.bit0) / g.tiles / 64 + 4), 1u << 30);
+      }
+      const uint32_t room = stage_room_any(g.type, g.dims, a, r.direction == 0);
+      a.img_words = std::min(g.img_words, room);
+      if (r.direction == 0 && g.img_words > room) {   // tiles larger than shared memory: one global slot per CTA
+        a.grid = (int)std::min<uint64_t>(g.tiles, (uint64_t)persistent_grid());
+        a.slot_words = g.img_words;
+        g.gimg_off = off;
+        g.gimg_bytes = (size_t)a.grid * g.img_words * 8;
+        off += (g.gimg_bytes + 255) & ~(size_t)255;
+      }
+    }
     gs.push_back(g);
   }
   lane->index_off.assign(reqs.size(), SIZE_MAX);
@@ -171,11 +215,18 @@ static cudaError_t launch_batch(Server* s, Lane* lane) {
     const Request& r0 = *reqs[g.idx[0]];
     const size_t planes = plane_bytes(r0.fi.esize, g.dims);
     if ((size_t)g.img_words * 8 + planes > kMaxTileSmem) return cudaErrorInvalidValue;  // refused at submit
+    const bool single = g.idx.size() == 1;
     LaunchArgs a;
-    std::memset(&a, 0, sizeof a);
-    a.one = r0.job;
-    a.jobs = (const Job*)(base + g.jobs_off);
-    a.njobs = (int)g.idx.size();
+    if (single) {
+      a = g.one;
+      a.one = lane->host_jobs[hj - 1];   // with its result and index pointers
+      if (g.gimg_bytes) a.gimg = (uint64_t*)(base + g.gimg_off);
+    } else {
+      std::memset(&a, 0, sizeof a);
+      a.one = r0.job;
+      a.jobs = (const Job*)(base + g.jobs_off);
+      a.njobs = (int)g.idx.size();
+    }
     const size_t t = (size_t)g.tiles + 1;
     char* p = base + g.scr_off;
     a.sc.ticket = (unsigned int*)(p + 32);
@@ -184,12 +235,14 @@ static cudaError_t launch_batch(Server* s, Lane* lane) {
     a.sc.side_cnt = (unsigned int*)(p + 64 + t * 24);
     a.sc.wait_cycles = wait_cycles();
     a.total_tiles = g.tiles;
-    a.use_ticket = 1;
-    // encode keeps whole tile images in shared memory (no global slots);
-    // decode stages only what fits the kernel's occupancy room
     const bool enc = reqs[g.idx[0]]->direction == 0;
-    a.img_words = enc ? g.img_words : std::min(g.img_words, stage_room_any(g.type, g.dims, a, false));
-    a.grid = (int)std::min<uint64_t>(g.tiles, (uint64_t)persistent_grid());
+    if (!single) {
+      a.use_ticket = 1;
+      // encode keeps whole tile images in shared memory (no global slots);
+      // decode stages only what fits the kernel's occupancy room
+      a.img_words = enc ? g.img_words : std::min(g.img_words, stage_room_any(g.type, g.dims, a, false));
+      a.grid = (int)std::min<uint64_t>(g.tiles, (uint64_t)persistent_grid());
+    }
     e = enc ? launch_encode_any(g.type, g.dims, a, lane->st) : launch_decode_any(g.type, g.dims, a, lane->st);
     if (e != cudaSuccess) return e;
   }
@@ -232,6 +285,7 @@ static void finish_lane(Server* s, Lane* lane) {
     }
     r.done = true;
     s->used -= r.cost;
+    s->served++;
   }
   cudaFreeAsync(lane->dev, lane->st);
   lane->dev = nullptr;
@@ -244,14 +298,15 @@ static void dispatcher(Server* s) {
   cudaSetDevice(s->device);
   const size_t kMaxBatch = 4096;
   std::unique_lock<std::mutex> lk(s->mu);
+  auto admissible = [&](const Lane& l) {
+    const auto& q = s->pending[l.cls];
+    return !l.busy && !q.empty() && s->used + q.front()->cost <= s->budget;
+  };
   for (;;) {
     s->cv.wait(lk, [&] {
       if (s->stop) return true;
       for (auto& l : s->lanes)
-        if (l->busy && l->finished) return true;
-      if (s->pending.empty()) return false;
-      for (auto& l : s->lanes)
-        if (!l->busy) return s->used + s->pending.front()->cost <= s->budget;
+        if ((l->busy && l->finished) || admissible(*l)) return true;
       return false;
     });
     bool any = false;
@@ -262,13 +317,16 @@ static void dispatcher(Server* s) {
       }
     if (any) s->cv.notify_all();
     for (auto& l : s->lanes) {
-      if (l->busy || s->pending.empty()) continue;
-      while (!s->pending.empty() && l->reqs.size() < kMaxBatch && s->used + s->pending.front()->cost <= s->budget) {
-        s->used += s->pending.front()->cost;
-        l->reqs.push_back(s->pending.front());
-        s->pending.pop_front();
+      if (l->busy) continue;
+      auto& q = s->pending[l->cls];
+      while (!q.empty() && l->reqs.size() < kMaxBatch && s->used + q.front()->cost <= s->budget) {
+        s->used += q.front()->cost;
+        l->reqs.push_back(q.front());
+        q.pop_front();
       }
       if (l->reqs.empty()) continue;
+      s->peak = std::max(s->peak, s->used);
+      s->batches++;
       l->busy = true;
       Lane* lane = l.get();
       lk.unlock();
@@ -289,8 +347,9 @@ static void dispatcher(Server* s) {
         s->cv.notify_all();
       }
     }
-    if (s->stop && s->pending.empty()) {
+    if (s->stop) {
       bool idle = true;
+      for (auto& q : s->pending) idle &= q.empty();
       for (auto& l : s->lanes) idle &= !l->busy;
       if (idle) break;
     }
@@ -316,6 +375,9 @@ zfp_gb300_server* zfp_gb300_server_create(size_t hbm_budget, int lanes) {
   for (int i = 0; i < lanes; i++) {
     auto l = std::make_unique<Lane>();
     l->server = s;
+    // one lane per class first (small, medium, large), the rest to the large class
+    l->cls = std::min(i, kClasses - 1);
+    s->lane_class_max = std::max(s->lane_class_max, l->cls);
     if (cudaStreamCreateWithFlags(&l->st, cudaStreamNonBlocking) != cudaSuccess) {
       fail("zfp_gb300_server_create: cannot create CUDA streams");
       for (auto& x : s->lanes) cudaStreamDestroy(x->st);
@@ -390,12 +452,14 @@ uint64_t zfp_gb300_server_submit(zfp_gb300_server* s, zfp_stream* z, const zfp_f
     fail("zfp_gb300_server_submit: request larger than the HBM budget");
     return 0;
   }
+  // a class without a lane of its own goes to the largest class that has one
+  r->cls = std::min(size_class((size_t)(fi.hi - fi.lo + 1) * fi.esize), s->lane_class_max);
   r->t_submit = Clock::now();
   {
     std::lock_guard<std::mutex> lk(s->mu);
     r->ticket = s->next_ticket++;
     s->live[r->ticket] = r;
-    s->pending.push_back(r);
+    s->pending[r->cls].push_back(r);
   }
   s->cv.notify_all();
   return r->ticket;
@@ -416,6 +480,15 @@ size_t zfp_gb300_server_wait(zfp_gb300_server* s, uint64_t ticket, double* secon
   if (seconds) *seconds = std::chrono::duration<double>(r->t_done - r->t_submit).count();
   if (!r->size) fail("zfp_gb300_server_wait: request failed");
   return r->size;
+}
+
+int zfp_gb300_server_stats(zfp_gb300_server* s, size_t* peak_bytes, uint64_t* batches, uint64_t* served) {
+  if (!s) return 0;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (peak_bytes) *peak_bytes = s->peak;
+  if (batches) *batches = s->batches;
+  if (served) *served = s->served;
+  return 1;
 }
 
 void zfp_gb300_server_free(zfp_gb300_server* s) {
