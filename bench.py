@@ -377,6 +377,8 @@ def bind_batch(lib):
     L.zfp_gb300_batch_finish.restype = C.c_int
     L.zfp_gb300_batch_finish.argtypes = [C.c_void_p, C.POINTER(C.c_size_t)]
     L.zfp_gb300_batch_free.argtypes = [C.c_void_p]
+    L.zfp_gb300_batch_get_tuning.restype = C.c_int
+    L.zfp_gb300_batch_get_tuning.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     return L
 
 
@@ -389,6 +391,10 @@ def batch_compare(lib, torch, stream, args):
     L = bind_batch(lib)
     count = 4096 if not args.small else 256
     arrays = workloads.batch_arrays(torch, count)
+    from zfp_gb300 import build as zbuild
+    loop = C.CDLL(zbuild.LOOP_LIB).zfp_gb300_loop_calls
+    loop.restype = C.c_size_t
+    loop.argtypes = [C.POINTER(capi.PZ), C.POINTER(capi.PF), C.c_size_t, C.c_int, C.c_int]
     raw = sum(x.numel() * 4 for x, _, _ in arrays)
 
     def objects(outs, bufs, use_out):
@@ -430,20 +436,17 @@ def batch_compare(lib, torch, stream, args):
     reps = max(2, min(args.steps, 5))
     result = {"arrays": count, "raw_bytes": raw}
     for direction, name in ((0, "compress"), (1, "decompress")):
-        # one launch per array
+        # one zfp_compress / zfp_decompress call per array, from a C loop
+        # over prebuilt objects (zfp_gb300/csrc/percall_loop.c)
         zs, fs, keep = objects(per_out, per_bufs, direction == 1)
-        fn = lib.zfp_compress if direction == 0 else lib.zfp_decompress
-        for z, f in zip(zs, fs):       # warm-up (and, for decompress, index lookups)
-            lib.zfp_stream_rewind(z)
-            assert fn(z, f)
+        za, fa = (capi.PZ * count)(*zs), (capi.PF * count)(*fs)
+        assert loop(za, fa, count, direction, 1) == 0, lib.zfp_gb300_last_error()   # warm-up, index lookups
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for _ in range(reps):
-            for z, f in zip(zs, fs):
-                lib.zfp_stream_rewind(z)
-                fn(z, f)
+        failed = loop(za, fa, count, direction, reps)
         torch.cuda.synchronize()
         per_s = (time.perf_counter() - t0) / reps
+        assert failed == 0
         close(zs, fs, keep)
         # one batched launch
         zs, fs, keep = objects(bat_out, bat_bufs, direction == 1)
@@ -452,6 +455,8 @@ def batch_compare(lib, torch, stream, args):
         sizes = (C.c_size_t * count)()
         assert L.zfp_gb300_batch_run(b, stream.cuda_stream)   # autotune + graph capture
         assert L.zfp_gb300_batch_finish(b, sizes)
+        tc, tsp = C.c_int(), C.c_int()
+        assert L.zfp_gb300_batch_get_tuning(b, C.byref(tc), C.byref(tsp))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(reps):
@@ -465,6 +470,7 @@ def batch_compare(lib, torch, stream, args):
             all(torch.equal(p.view(torch.int32), q.view(torch.int32)) for p, q in zip(per_out, bat_out))
         result[name] = {"per_array_gbs": round(raw / per_s / 1e9, 2), "batched_gbs": round(raw / bat_s / 1e9, 2),
                         "speedup": round(per_s / bat_s, 2), "bit_identical": bool(same),
+                        "tuned": {"ctas_per_sm": tc.value, "staging_pct": tsp.value},
                         "per_array_ms": round(per_s * 1e3, 3), "batched_ms": round(bat_s * 1e3, 3)}
     return result
 

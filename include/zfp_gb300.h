@@ -84,9 +84,16 @@ zfp_bool zfp_gb300_batch_finish(zfp_gb300_batch* batch, size_t* sizes);
 
 void zfp_gb300_batch_free(zfp_gb300_batch* batch);
 
-/* CTAs per SM of the persistent batch launch; 0 (default) picks the value
- * the built-in autotuner measured fastest for this batch on its first run. */
+/* CTAs per SM of the persistent batch launch; 0 (default) lets the built-in
+ * autotuner choose on the batch's first run: it times CTAs per SM (1, 2, 3,
+ * 4, 6, 8) against how much of each CTA's shared memory stages tile images
+ * and stream words (all of the room its occupancy leaves, or half), three
+ * runs each, and keeps the best median.  A value set here uses full staging. */
 zfp_bool zfp_gb300_batch_set_ctas_per_sm(zfp_gb300_batch* batch, int ctas_per_sm);
+
+/* The launch shape in use once the batch has run (zfp_false before): CTAs per
+ * SM and the staging share in percent. */
+zfp_bool zfp_gb300_batch_get_tuning(const zfp_gb300_batch* batch, int* ctas_per_sm, int* staging_pct);
 
 /* ---- serving: continuous batching of independent requests --------------
  * A server runs compress / decompress requests on device-resident fields

@@ -11,6 +11,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libzfp_gb300.so")
+LOOP_LIB = os.path.join(HERE, "libzfp_gb300_loop.so")   # per-call C client of the API (benchmark arm)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 CFLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-O3"]
@@ -45,6 +46,8 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     """Compile the CUDA library if any source changed; return its path."""
     deps = _deps()
     if not force and not _newer(LIB, deps):
+        if _newer(LOOP_LIB, [LIB, os.path.join(CSRC, "percall_loop.c")]):
+            build_loop()
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     extra = extra or []
@@ -56,9 +59,20 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_loop()
     if verbose:
         print("built", LIB)
     return LIB
+
+
+def build_loop() -> str:
+    """libzfp_gb300_loop.so: csrc/percall_loop.c, a C client linked against the library."""
+    src = os.path.join(CSRC, "percall_loop.c")
+    r = subprocess.run([os.environ.get("CC", "gcc"), "-O2", "-std=c99", "-fPIC", "-shared", "-o", LOOP_LIB, src,
+                        "-L", HERE, "-lzfp_gb300", "-Wl,-rpath,$ORIGIN"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"gcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+    return LOOP_LIB
 
 
 if __name__ == "__main__":

@@ -8,7 +8,11 @@
 // persistent grid: CTAs take tiles from a counter in order, which keeps the
 // look-back of variable-rate jobs deadlock-free and spreads uneven work over
 // all SMs.  The launches are captured once in a CUDA graph and replayed.
-// CTAs-per-SM of the persistent grid is autotuned on the first run.
+// The first run autotunes the persistent grid's CTAs per SM and how much of
+// each CTA's shared memory stages tile images / stream words (all of the
+// room its occupancy leaves, or half of it, which lets more CTAs share an
+// SM while more tiles go through global memory): every candidate is timed
+// three times and the one with the best median kept.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -28,7 +32,7 @@ struct BatchGroup {
   std::vector<size_t> members;
   uint32_t total_tiles = 0;
   uint32_t tile_words = 0;     // largest tile image of any member
-  uint32_t img_words = 0;      // shared-memory part (see plan_launch in gpu_codec.cu)
+  uint32_t img_words = 0;      // shared-memory part at full staging (see plan_launch in gpu_codec.cu)
   bool needs_ticket = false;
   Job* d_jobs = nullptr;       // device copy of this group's jobs (sorted by tile0)
   LaunchScratch sc{};
@@ -57,6 +61,7 @@ struct zfp_gb300_batch {
   cudaGraphExec_t graph = nullptr;
   cudaStream_t graph_stream = nullptr;
   int ctas_per_sm = 0;
+  int stage_pct = 100;                 // share of the staging room used (100 or 50)
   bool tuned = false;
 };
 
@@ -64,7 +69,7 @@ namespace zg {
 
 static int sm_count() { return persistent_grid() / 4; }
 
-static cudaError_t enqueue(zfp_gb300_batch* b, cudaStream_t st, int ctas_per_sm) {
+static cudaError_t enqueue(zfp_gb300_batch* b, cudaStream_t st, int ctas_per_sm, int stage_pct) {
   for (auto& g : b->groups) {
     cudaError_t e = cudaMemsetAsync(g.scratch, 0, g.scratch_bytes, st);
     if (e != cudaSuccess) return e;
@@ -76,10 +81,16 @@ static cudaError_t enqueue(zfp_gb300_batch* b, cudaStream_t st, int ctas_per_sm)
     a.sc = g.sc;
     a.total_tiles = g.total_tiles;
     a.use_ticket = 1;
+    // less staging only where the tiles it no longer holds have somewhere
+    // to go: the decoder reads them from the stream, the encoder needs its
+    // global slots
     a.img_words = g.img_words;
+    if (stage_pct < 100 && (b->direction == 1 || g.gimg))
+      a.img_words = std::max<uint32_t>(std::min<uint32_t>(64, g.img_words),
+                                       (uint32_t)((uint64_t)g.img_words * stage_pct / 100));
     const int grid = std::max(1, sm_count() * ctas_per_sm);
     a.grid = (int)std::min<uint64_t>(g.total_tiles, (uint64_t)grid);
-    if (g.gimg) {
+    if (g.gimg && g.tile_words > a.img_words) {
       a.gimg = g.gimg;
       a.slot_words = g.tile_words;
       a.grid = (int)std::min<uint64_t>((uint64_t)a.grid, g.gimg_words / g.tile_words);
@@ -256,7 +267,7 @@ zfp_gb300_batch* zfp_gb300_batch_create(zfp_stream* const* streams, const zfp_fi
     probe.jobs = g.d_jobs;
     const uint32_t room = stage_room_any(g.type, g.dims, probe, b->direction == 0);
     g.img_words = std::min(g.tile_words, room);
-    if (b->direction == 0 && g.tile_words > room) {
+    if (b->direction == 0 && g.tile_words > room / 2) {   // global slots for tiles that outgrow the staging
       g.gimg_words = (size_t)persistent_grid() * 2 * g.tile_words;
       if ((e = cudaMalloc((void**)&g.gimg, g.gimg_words * 8)) != cudaSuccess) {
         fail_cuda("zfp_gb300_batch_create: staging", e);
@@ -272,11 +283,19 @@ zfp_gb300_batch* zfp_gb300_batch_create(zfp_stream* const* streams, const zfp_fi
 zfp_bool zfp_gb300_batch_set_ctas_per_sm(zfp_gb300_batch* b, int ctas_per_sm) {
   if (!b || ctas_per_sm < 0 || ctas_per_sm > 16) return zfp_false;
   b->ctas_per_sm = ctas_per_sm;
+  b->stage_pct = 100;
   b->tuned = ctas_per_sm > 0;
   if (b->graph) {
     cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
   }
+  return zfp_true;
+}
+
+zfp_bool zfp_gb300_batch_get_tuning(const zfp_gb300_batch* b, int* ctas_per_sm, int* staging_pct) {
+  if (!b || !b->tuned) return zfp_false;
+  if (ctas_per_sm) *ctas_per_sm = b->ctas_per_sm;
+  if (staging_pct) *staging_pct = b->stage_pct;
   return zfp_true;
 }
 
@@ -293,35 +312,42 @@ zfp_bool zfp_gb300_batch_run(zfp_gb300_batch* b, void* cuda_stream) {
     st = b->own_stream;
   }
   if (!b->tuned) {
-    // autotune the persistent grid: time each candidate once, keep the fastest
-    const int candidates[] = {1, 2, 3, 4, 6, 8};
+    // autotune: CTAs per SM x staging depth, three timed runs each, best median
+    const int ctas[] = {1, 2, 3, 4, 6, 8};
+    const int stages[] = {100, 50};
     float best = 1e30f;
-    int pick = 4;
+    int pick_c = 4, pick_s = 100;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    if ((e = enqueue(b, st, 4)) != cudaSuccess) {  // warm-up (also sets kernel attributes before capture)
+    if ((e = enqueue(b, st, 4, 100)) != cudaSuccess) {  // warm-up (also sets kernel attributes before capture)
       fail_cuda("zfp_gb300_batch_run", e);
       return zfp_false;
     }
-    for (int c : candidates) {
-      cudaEventRecord(e0, st);
-      if ((e = enqueue(b, st, c)) != cudaSuccess) {
-        fail_cuda("zfp_gb300_batch_run", e);
-        return zfp_false;
+    for (int sp : stages)
+      for (int c : ctas) {
+        float t[3];
+        for (float& ms : t) {
+          cudaEventRecord(e0, st);
+          if ((e = enqueue(b, st, c, sp)) != cudaSuccess) {
+            fail_cuda("zfp_gb300_batch_run", e);
+            return zfp_false;
+          }
+          cudaEventRecord(e1, st);
+          cudaEventSynchronize(e1);
+          cudaEventElapsedTime(&ms, e0, e1);
+        }
+        std::sort(t, t + 3);
+        if (t[1] < best) {
+          best = t[1];
+          pick_c = c;
+          pick_s = sp;
+        }
       }
-      cudaEventRecord(e1, st);
-      cudaEventSynchronize(e1);
-      float ms = 0;
-      cudaEventElapsedTime(&ms, e0, e1);
-      if (ms < best) {
-        best = ms;
-        pick = c;
-      }
-    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    b->ctas_per_sm = pick;
+    b->ctas_per_sm = pick_c;
+    b->stage_pct = pick_s;
     b->tuned = true;
   }
   if (!b->graph || b->graph_stream != st) {
@@ -334,7 +360,7 @@ zfp_bool zfp_gb300_batch_run(zfp_gb300_batch* b, void* cuda_stream) {
       fail_cuda("zfp_gb300_batch_run: capture", e);
       return zfp_false;
     }
-    cudaError_t le = enqueue(b, st, b->ctas_per_sm);
+    cudaError_t le = enqueue(b, st, b->ctas_per_sm, b->stage_pct);
     e = cudaStreamEndCapture(st, &g);
     if (le != cudaSuccess || e != cudaSuccess) {
       fail_cuda("zfp_gb300_batch_run: capture", le != cudaSuccess ? le : e);
