@@ -54,6 +54,7 @@ def parse_args():
     p.add_argument("--no-batch", action="store_true")
     p.add_argument("--no-serve", action="store_true")
     p.add_argument("--no-refcuda", action="store_true")
+    p.add_argument("--no-config3", action="store_true")
     p.add_argument("--only", default=None,
                    help="profiling: run one kernel, FIELD:MODE:DIR (e.g. f32:rate:c), --steps times")
     p.add_argument("--shape", default=None, help="profiling: field shape Z,Y,X for --only")
@@ -317,12 +318,19 @@ def gpu_arm(args):
     if not args.no_refcuda:
         ref_cuda = reference_cuda_column(fields, one, torch, reps)
 
+    # the edge-shape configuration at full size
+    cfg3 = None
+    if not args.no_config3:
+        torch.cuda.empty_cache()
+        cfg3 = config3_timings(lib, torch, max(3, min(args.steps, 10)), stream.cuda_stream)
+
     # end to end: host pinned buffers through the same C API (synchronous calls)
     ratios = {f"{fd['name']}_{m}": round(fd["raw"] / fd["sizes"][m], 3) for fd in fields for m, _ in MODES}
     shapes = [list(fd["shape"]) for fd in fields]
     e2e = None
     if not args.no_e2e:
         e2e = e2e_run(lib, torch, codec, fields, args)
+        e2e["host_link"] = host_link(torch)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -357,6 +365,7 @@ def gpu_arm(args):
                                                          "hbm_frac": round(r["hbm_gbs"] / peak, 4)} for r in fixed},
             "per_kernel": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in r.items()} for r in per],
             "reference_cuda": ref_cuda,
+            "config3": cfg3,
             "checks": checks,
             "compression_ratio": ratios,
             "batch": batch,
@@ -663,6 +672,112 @@ def serve_compare(lib, torch, args, count=20000, rate=6000.0):
 def zfp_gb300_last():
     import zfp_gb300
     return zfp_gb300.last_error()
+
+
+def config3_timings(lib, torch, reps, stream_handle):
+    """The edge-shape configuration at full size, each case compressed and
+    decompressed alone on the device (CUDA events, `reps` calls): (a) 2D
+    float64 16384^2, (b) 4D float32 64^4, (c) 3D float32 383x257x129, (d) the
+    transposed strided view of (c) with strides (257*129, 1, 257), in fixed
+    rate 12 and fixed precision 24; (e) 3D int32 256^3 uniform in
+    [-2^20, 2^20), reversible.  Raw GB/s and (raw + stream) bytes per second
+    against the HBM peak."""
+    from zfp_gb300 import capi, synth
+    peak, _ = peak_hbm()
+    stream = torch.cuda.current_stream()
+    cases = []
+    c = synth.smooth_field_torch((129, 257, 383), torch.float32, seed=4, noise=1e-2)
+    mem = c.permute(2, 0, 1).contiguous()          # memory order x (slowest), z, y (fastest)
+    view = mem.as_strided((129, 257, 383), (257, 1, 257 * 129))
+    for mode, arg in (("rate", 12), ("precision", 24)):
+        cases.append(("b_4d_f32_64^4", lambda: synth.smooth_field_torch((64, 64, 64, 64), torch.float32, seed=3,
+                                                                         noise=1e-2), mode, arg))
+        cases.append(("c_3d_f32_383x257x129", lambda: c, mode, arg))
+        cases.append(("d_strided_view_of_c", lambda: view, mode, arg))
+        cases.append(("a_2d_f64_16384^2", lambda: synth.smooth_field_torch((16384, 16384), torch.float64, seed=5,
+                                                                            noise=1e-2), mode, arg))
+    cases.append(("e_3d_i32_256^3", lambda: torch.randint(-(1 << 20), 1 << 20, (256, 256, 256), dtype=torch.int32,
+                                                           device="cuda", generator=torch.Generator(device="cuda")
+                                                           .manual_seed(3)), "reversible", None))
+    out = []
+    for name, make, mode, arg in cases:
+        x = make()
+        ztype = {torch.float32: capi.TYPE_FLOAT, torch.float64: capi.TYPE_DOUBLE, torch.int32: capi.TYPE_INT32}[x.dtype]
+        n, st = tuple(reversed(x.shape)), tuple(reversed(x.stride()))
+        raw = x.numel() * x.element_size()
+        y = torch.empty(x.shape, dtype=x.dtype, device="cuda")
+        cap = raw * 2 + (1 << 20)
+        buf = torch.zeros(cap // 8, dtype=torch.int64, device="cuda")
+        bs = lib.stream_open(buf.data_ptr(), cap)
+        z = lib.zfp_stream_open(bs)
+        capi.set_mode(lib, z, mode, arg, ztype, x.dim())
+        lib.zfp_stream_set_execution(z, capi.EXEC_CUDA)
+        lib.zfp_gb300_stream_set_cuda_stream(z, stream_handle)
+        fc = capi.make_field(lib, x.data_ptr(), ztype, n, st)
+        fd = capi.make_field(lib, y.data_ptr(), ztype, n, st)   # same strides: the decoded view lands the same way
+        row = {"case": name, "mode": mode, "arg": arg, "raw_bytes": raw}
+        size = 0
+        for direction, f in (("compress", fc), ("decompress", fd)):
+            fn = lib.zfp_compress if direction == "compress" else lib.zfp_decompress
+            lib.zfp_stream_rewind(z)
+            size = fn(z, f)
+            assert size, f"{name} {mode} {direction}: {zfp_gb300_last()}"
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                lib.zfp_stream_rewind(z)
+                fn(z, f)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            row[direction] = {"ms": round(ms, 4), "raw_gbs": round(raw / ms / 1e6, 1),
+                              "hbm_frac": round((raw + size) / ms / 1e6 / peak, 4)}
+        row["stream_bytes"] = size
+        if mode == "reversible":
+            row["lossless"] = bool(torch.equal(x, y))
+        lib.zfp_field_free(fc)
+        lib.zfp_field_free(fd)
+        lib.zfp_stream_close(z)
+        lib.stream_close(bs)
+        out.append(row)
+        del x, y, buf
+    return out
+
+
+def host_link(torch, nbytes=1 << 30, reps=5):
+    """Copy-engine bandwidth between pinned host memory and HBM (the ceiling
+    of the e2e measurement, whose calls read and write pinned buffers over
+    the same link): host-to-device, device-to-host, and both at once on two
+    CUDA streams.  CUDA events, best of `reps`."""
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    h2 = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    d2 = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def timed(fn):
+        best = 1e30
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t0)
+        return best
+
+    def both():
+        with torch.cuda.stream(s1):
+            d.copy_(h, non_blocking=True)
+        with torch.cuda.stream(s2):
+            h2.copy_(d2, non_blocking=True)
+
+    t_h2d = timed(lambda: d.copy_(h, non_blocking=True))
+    t_d2h = timed(lambda: h2.copy_(d2, non_blocking=True))
+    t_both = timed(both)
+    return {"bytes": nbytes, "h2d_gbs": round(nbytes / t_h2d / 1e9, 1), "d2h_gbs": round(nbytes / t_d2h / 1e9, 1),
+            "bidirectional_gbs": round(2 * nbytes / t_both / 1e9, 1),
+            "how": "pinned host <-> device copies of 1 GiB (torch copy_ on the copy engines), best of 5"}
 
 
 def e2e_run(lib, torch, codec, fields, args):
