@@ -122,7 +122,7 @@ uint64_t compress_t(const Geom& g, const zg::BlockParams& p, const void* data, u
         continue;
       }
     }
-    zg::encode_block<S, D>(out, p, raw);
+    zg::encode_block<S, D>(out, p, raw, zg::kGroupCodeHost.e);
   }
   return out.pos;
 }

@@ -865,65 +865,227 @@ ZG_HD unsigned decode_planes(Source& in, unsigned budget, unsigned maxprec, Plan
   return budget - bits;
 }
 
-// Rolled coder for 4D blocks (256 coefficients), planes formed on the fly.
-template <typename U, class Sink>
-ZG_HD unsigned encode_planes_wide(Sink& out, unsigned budget, unsigned maxprec, const U (&u)[256]) {
-  constexpr int P = 8 * sizeof(U), N = 256;
-  const int kmin = (unsigned)P > maxprec ? P - (int)maxprec : 0;
-  unsigned bits = budget, n = 0;
-  for (int k = P - 1; k >= kmin && bits; k--) {
-    uint64_t pl[4] = {0, 0, 0, 0};
-    for (int i = 0; i < N; i++) pl[i >> 6] |= (uint64_t)((u[i] >> k) & 1u) << (i & 63);
-    const unsigned m = n < bits ? n : bits;
-    for (unsigned i = 0; i < m; i += 64) {
-      const unsigned c = m - i < 64 ? m - i : 64;
-      out.put(low_bits(pl[i >> 6], c), c);
+// group-test code of bytes and 16-bit chunks (see the table-driven coder below)
+// E(b) in bits 0-15 (every one of the byte b followed by a '1'), popc(b) in bits 16-19
+ZG_HD constexpr uint32_t group_code_entry(uint32_t b) {
+  uint32_t e = 0, j = 0;
+  for (uint32_t p = 0; p < 8; p++)
+    if ((b >> p) & 1u) {
+      e |= 3u << (p + j);
+      j++;
     }
-    bits -= m;
-    while (bits && n < (unsigned)N) {
-      bits--;
-      unsigned p = n;                             // next one at or after n
-      while (p < (unsigned)N) {
-        const uint64_t w = pl[p >> 6] >> (p & 63);
-        if (w) { p += ctz64(w); break; }
-        p = (p | 63) + 1;
-      }
-      if (p >= (unsigned)N) { out.put(0, 1); break; }
-      out.put(1, 1);
-      for (; bits && n < (unsigned)N - 1; n++) {
-        bits--;
-        const unsigned b = n == p;
-        out.put(b, 1);
-        if (b) break;
-      }
-      n++;
-    }
-  }
-  return budget - bits;
+  return e | (j << 16);
 }
 
-template <typename U, class Source>
-ZG_HD unsigned decode_planes_wide(Source& in, unsigned budget, unsigned maxprec, U (&u)[256]) {
-  constexpr int P = 8 * sizeof(U), N = 256;
+struct GroupCodeTable {
+  uint32_t e[256];
+};
+
+constexpr GroupCodeTable make_group_code_table() {
+  GroupCodeTable t{};
+  for (uint32_t b = 0; b < 256; b++) t.e[b] = group_code_entry(b);
+  return t;
+}
+
+constexpr GroupCodeTable kGroupCodeHost = make_group_code_table();
+
+// code of 16 group-test bits c of a plane (at most 32 bits), length in len;
+// `last`: the plane's last one is in this chunk, at position t of it, and
+// `implied` says whether it is the block's last coefficient (then it and its
+// test are not written; otherwise the test after it is negative)
+ZG_HD uint32_t group_chunk(uint32_t c, const uint32_t* gtab, bool last, unsigned t, bool implied, unsigned& len) {
+  const uint32_t e0 = gtab[c & 0xffu], e1 = gtab[c >> 8];
+  const unsigned p0 = e0 >> 16, pc = p0 + (e1 >> 16);
+  uint32_t code = (e0 & 0xffffu) | ((e1 & 0xffffu) << (8 + p0));
+  len = 16 + pc;
+  if (last) {
+    if (implied) {
+      len = t + pc - 1;
+      code &= len < 32 ? (1u << len) - 1 : ~0u;
+    } else {
+      len = t + pc + 1;
+      code &= ~(1u << (len - 1));
+    }
+  }
+  return code;
+}
+
+// 4D blocks (256 coefficients): bit planes of four 64-bit words, plane k at
+// pl[4k .. 4k+3] with coefficient i at bit i % 64 of word i / 64, formed and
+// taken apart with the same 32x32 register transposes as 1-3D blocks (eight
+// groups of 32 coefficients per 32-bit half of the values).
+
+template <typename U, int P>
+ZG_HD void make_planes_wide(const U (&u)[256], uint64_t (&pl)[4 * P]) {
+  for (int grp = 0; grp < 8; grp++) {
+#pragma unroll
+    for (int half = 0; half < P / 32; half++) {
+      uint32_t a[32];
+#pragma unroll
+      for (int i = 0; i < 32; i++) a[i] = (uint32_t)((uint64_t)u[32 * grp + i] >> (32 * half));
+      transpose32(a);
+#pragma unroll
+      for (int k = 0; k < 32; k++) {
+        uint64_t& w = pl[4 * (32 * half + k) + grp / 2];
+        if (grp & 1) w |= (uint64_t)a[k] << 32;
+        else w = a[k];
+      }
+    }
+  }
+}
+
+template <typename U, int P>
+ZG_HD void take_planes_wide(const uint64_t (&pl)[4 * P], U (&u)[256]) {
+  for (int grp = 0; grp < 8; grp++) {
+    U acc[32];
+#pragma unroll
+    for (int i = 0; i < 32; i++) acc[i] = 0;
+#pragma unroll
+    for (int half = 0; half < P / 32; half++) {
+      uint32_t a[32];
+#pragma unroll
+      for (int k = 0; k < 32; k++) a[k] = (uint32_t)(pl[4 * (32 * half + k) + grp / 2] >> (32 * (grp & 1)));
+      transpose32(a);
+#pragma unroll
+      for (int i = 0; i < 32; i++) acc[i] |= (U)((uint64_t)a[i] << (32 * half));
+    }
+#pragma unroll
+    for (int i = 0; i < 32; i++) u[32 * grp + i] = acc[i];
+  }
+}
+
+// bits [pos, pos + 16) of a 256-bit plane (zeros past its end)
+ZG_HD uint32_t plane_bits16(const uint64_t* x, unsigned pos) {
+  const unsigned w = pos >> 6, o = pos & 63;
+  uint64_t v = x[w] >> o;
+  if (o > 48 && w < 3) v |= x[w + 1] << (64 - o);
+  return (uint32_t)v & 0xffffu;
+}
+
+// highest set bit of a 256-bit plane, or -1
+ZG_HD int plane_top(const uint64_t* x) {
+  for (int w = 3; w >= 0; w--)
+    if (x[w]) return 64 * w + 63 - clz64(x[w]);
+  return -1;
+}
+
+// ones of a 256-bit plane in [lo, hi]
+ZG_HD unsigned plane_popc(const uint64_t* x, unsigned lo, unsigned hi) {
+  unsigned c = 0;
+  for (unsigned w = lo >> 6; w <= hi >> 6; w++) {
+    uint64_t v = x[w];
+    if (w == lo >> 6) v &= ~0ull << (lo & 63);
+    if (w == hi >> 6 && (hi & 63) != 63) v &= (2ull << (hi & 63)) - 1;
+    c += (unsigned)popc64(v);
+  }
+  return c;
+}
+
+// The coder of emit_block_seq (the same group-test expansion, a 16-bit
+// chunk at a time from the byte table) over 256-bit planes: per plane the
+// verbatim bits in 64-bit pieces, the opening test, then the chunks up to
+// the top one.  With `count` nothing is written and only the length is
+// returned: a plane's length is O(1) from its top one and popcount.
+template <int P, bool kCount, class Sink>
+ZG_HD unsigned code_planes_wide(Sink& out, unsigned budget, unsigned maxprec, const uint64_t* pl,
+                                const uint32_t* gtab) {
+  constexpr unsigned N = 256;
+  const int kmin = (unsigned)P > maxprec ? P - (int)maxprec : 0;
+  unsigned left = budget, n = 0;
+  auto put = [&](uint64_t v, unsigned len) {   // cut at the budget; false once it is spent
+    if (len >= left) {
+      if (!kCount) out.put(low_bits(v, left), left);
+      left = 0;
+      return false;
+    }
+    if (!kCount) out.put(v, len);
+    left -= len;
+    return true;
+  };
+  for (int k = P - 1; k >= kmin && left; k--) {
+    const uint64_t* x = pl + 4 * k;
+    int top = plane_top(x);
+    if (top < (int)n) top = -1;                  // no coefficient becomes significant
+    if (kCount) {
+      unsigned len = n;
+      if (n < N) {
+        len += 1;
+        if (top >= 0) {
+          const unsigned m = plane_popc(x, n, (unsigned)top);
+          len += (unsigned)top == N - 1 ? (unsigned)top - n + m - 1 : (unsigned)top - n + 1 + m;
+        }
+      }
+      if (len >= left) return budget;
+      left -= len;
+      if (top >= 0) n = (unsigned)top + 1;
+      continue;
+    }
+    bool more = true;
+    for (unsigned w = 0; w * 64 < n && more; w++) {
+      const unsigned c = n - 64 * w < 64 ? n - 64 * w : 64;
+      more = put(low_bits(x[w], c), c);
+    }
+    if (!more) break;
+    if (n >= N) continue;
+    if (!put(top >= 0, 1)) break;
+    if (top < 0) continue;
+    const bool implied = (unsigned)top == N - 1;
+    const unsigned rem = (unsigned)top - n;
+    for (unsigned c = 0; more; c += 16) {
+      unsigned clen;
+      const uint32_t code = group_chunk(plane_bits16(x, n + c), gtab, rem < c + 16, rem - c, implied, clen);
+      more = put(code, clen) && rem >= c + 16;
+    }
+    if (!left) break;
+    n = (unsigned)top + 1;
+  }
+  return budget - left;
+}
+
+// The decoder of src/template/decode.c:80-278 over 256-bit planes: verbatim
+// bits in 64-bit pieces, then one significance event at a time, each scan
+// 64 bits per peek (4D blocks have up to 255 coefficients to scan).
+template <int P, class Source>
+ZG_HD unsigned decode_planes_wide(Source& in, unsigned budget, unsigned maxprec, uint64_t (&pl)[4 * P]) {
+  constexpr unsigned N = 256;
   const int kmin = (unsigned)P > maxprec ? P - (int)maxprec : 0;
   unsigned bits = budget, n = 0;
-  for (int i = 0; i < N; i++) u[i] = 0;
+  for (int k = 0; k < 4 * P; k++) pl[k] = 0;
   for (int k = P - 1; k >= kmin && bits; k--) {
+    uint64_t* x = pl + 4 * k;
     const unsigned m = n < bits ? n : bits;
-    for (unsigned i = 0; i < m; i += 64) {
-      const unsigned c = m - i < 64 ? m - i : 64;
-      const uint64_t v = in.read(c);
-      for (unsigned j = 0; j < c; j++) u[i + j] += (U)((v >> j) & 1u) << k;
+    for (unsigned w = 0; w * 64 < m; w++) {
+      const unsigned c = m - 64 * w < 64 ? m - 64 * w : 64;
+      x[w] = in.read(c);
     }
     bits -= m;
-    while (bits && n < (unsigned)N) {
+    while (bits && n < N) {
       bits--;
-      if (!in.read(1)) break;
-      for (; bits && n < (unsigned)N - 1; n++) {
-        bits--;
-        if (in.read(1)) break;
+      const bool positive = in.peek64() & 1u;
+      in.skip(1);
+      if (!positive) break;                      // rest of the plane is zero
+      // scan at most cap coefficient bits for the next one; none: it is
+      // implied (the last coefficient) or the budget ended inside the test
+      const unsigned cap = N - 1 - n < bits ? N - 1 - n : bits;
+      unsigned z = 0;
+      bool found = false;
+      while (z < cap) {
+        const unsigned c = cap - z < 64 ? cap - z : 64;
+        uint64_t w = in.peek64();
+        if (c < 64) w |= uint64_t(1) << c;
+        const unsigned t = w ? ctz64(w) : 64u;
+        if (t < c) {
+          in.skip(t + 1);
+          z += t;
+          found = true;
+          break;
+        }
+        in.skip(c);
+        z += c;
       }
-      u[n] += (U)1 << k;
+      bits -= z + (found ? 1u : 0u);
+      n += z;
+      x[n >> 6] |= uint64_t(1) << (n & 63);
       n++;
     }
   }
@@ -1001,7 +1163,10 @@ ZG_HD unsigned uncode_coeffs(Source& in, unsigned budget, unsigned maxprec,
     take_planes<N>(pl, u);
     return bits;
   } else {
-    return decode_planes_wide<U>(in, budget, maxprec, u);
+    uint64_t pl[4 * P];
+    const unsigned bits = decode_planes_wide<P>(in, budget, maxprec, pl);
+    take_planes_wide<U, P>(pl, u);
+    return bits;
   }
 }
 
@@ -1372,29 +1537,6 @@ ZG_HD unsigned emit_block(Sink& out, const BlockHead& h, const uint64_t* plane, 
 // budget, which truncates the code exactly where the reference's per-bit
 // budget stops its coder (src/template/encode.c:92-256).
 
-// E(b) in bits 0-15 (every one of the byte b followed by a '1'), popc(b) in bits 16-19
-ZG_HD constexpr uint32_t group_code_entry(uint32_t b) {
-  uint32_t e = 0, j = 0;
-  for (uint32_t p = 0; p < 8; p++)
-    if ((b >> p) & 1u) {
-      e |= 3u << (p + j);
-      j++;
-    }
-  return e | (j << 16);
-}
-
-struct GroupCodeTable {
-  uint32_t e[256];
-};
-
-constexpr GroupCodeTable make_group_code_table() {
-  GroupCodeTable t{};
-  for (uint32_t b = 0; b < 256; b++) t.e[b] = group_code_entry(b);
-  return t;
-}
-
-constexpr GroupCodeTable kGroupCodeHost = make_group_code_table();
-
 template <int P, int N, class Sink>
 ZG_HD unsigned emit_block_seq(Sink& out, const BlockHead& h, const uint64_t* plane, int stride, const uint32_t* gtab) {
   out.put(h.hdr, h.hdr_bits);
@@ -1471,28 +1613,37 @@ ZG_HD unsigned emit_block_seq(Sink& out, const BlockHead& h, const uint64_t* pla
   return bits;
 }
 
-// 4D blocks keep the rolled wide coder over the coefficient array
+// 4D blocks: the header, and the coefficients as 256-bit bit planes
 template <typename S>
 struct WideCode {
   using U = typename Traits<S>::UInt;
+  static constexpr int P = 8 * sizeof(U);
   BlockHead h;
-  U u[256];
+  uint64_t pl[4 * P];
+  ZG_HD void set(const U (&u)[256]) {
+    if (h.coded) make_planes_wide<U, P>(u, pl);
+  }
   template <class Sink>
-  ZG_HD unsigned emit(Sink& out) const {
+  ZG_HD unsigned emit(Sink& out, const uint32_t* gtab) const {
     out.put(h.hdr, h.hdr_bits);
     unsigned bits = h.hdr_bits;
-    if (h.coded) bits += encode_planes_wide<U>(out, h.budget, h.maxprec, u);
+    if (h.coded) bits += code_planes_wide<P, false>(out, h.budget, h.maxprec, pl, gtab);
     if (bits < h.pad_to) { out.pad(h.pad_to - bits); bits = h.pad_to; }
     return bits;
   }
   ZG_HD unsigned length() const {
     CountSink c;
-    return emit(c);
+    unsigned bits = h.hdr_bits;
+    if (h.coded) bits += code_planes_wide<P, true>(c, h.budget, h.maxprec, pl, nullptr);
+    return bits > h.pad_to ? bits : h.pad_to;
   }
 };
 
+// whole-block encoder (one significance event per put for 1-3D blocks; gtab:
+// the group-code table, used by 4D blocks)
 template <typename S, int D, class Sink>
-ZG_HD unsigned encode_block(Sink& out, const BlockParams& p, const typename Traits<S>::Bits (&raw)[1 << (2 * D)]) {
+ZG_HD unsigned encode_block(Sink& out, const BlockParams& p, const typename Traits<S>::Bits (&raw)[1 << (2 * D)],
+                            const uint32_t* gtab) {
   using U = typename Traits<S>::UInt;
   constexpr int N = 1 << (2 * D);
   if constexpr (N <= 64) {
@@ -1504,8 +1655,10 @@ ZG_HD unsigned encode_block(Sink& out, const BlockParams& p, const typename Trai
     return emit_block<8 * sizeof(U), N>(out, h, plane, 1);
   } else {
     WideCode<S> wc;
-    prepare_coeffs<S, D>(wc.h, p, raw, wc.u);
-    return wc.emit(out);
+    U u[256];
+    prepare_coeffs<S, D>(wc.h, p, raw, u);
+    wc.set(u);
+    return wc.emit(out, gtab);
   }
 }
 

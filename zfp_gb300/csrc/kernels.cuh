@@ -420,7 +420,9 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
       if (h.coded) store_planes<N, kSel == kLossyFloor>(u, my_planes, kTile, h.maxprec);
       len = fixed ? job.maxbits : block_bits<P, N>(h, my_planes, kTile);
     } else {
-      prepare_coeffs<S, D, kSel>(wc.h, p, raw, wc.u);
+      U u[N];
+      prepare_coeffs<S, D, kSel>(wc.h, p, raw, u);
+      wc.set(u);
       len = fixed ? job.maxbits : wc.length();
     }
   }
@@ -445,7 +447,7 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
       out.finish();
     } else {
       SmemSink out{img, excl >> 6, excl & 63u, 0ull, true, nw, &job.result->status};
-      wc.emit(out);
+      wc.emit(out, gtab);
       out.finish();
     }
   }
