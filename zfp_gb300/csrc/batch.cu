@@ -92,8 +92,8 @@ static cudaError_t enqueue(zfp_gb300_batch* b, cudaStream_t st, int ctas_per_sm,
     a.grid = (int)std::min<uint64_t>(g.total_tiles, (uint64_t)grid);
     if (g.gimg && g.tile_words > a.img_words) {
       a.gimg = g.gimg;
-      a.slot_words = g.tile_words;
-      a.grid = (int)std::min<uint64_t>((uint64_t)a.grid, g.gimg_words / g.tile_words);
+      a.slot_words = slot_stride(g.tile_words);
+      a.grid = (int)std::min<uint64_t>((uint64_t)a.grid, g.gimg_words / a.slot_words);
     }
     e = b->direction == 0 ? launch_encode_any(g.type, g.dims, a, st) : launch_decode_any(g.type, g.dims, a, st);
     if (e != cudaSuccess) return e;
@@ -268,7 +268,7 @@ zfp_gb300_batch* zfp_gb300_batch_create(zfp_stream* const* streams, const zfp_fi
     const uint32_t room = stage_room_any(g.type, g.dims, probe, b->direction == 0);
     g.img_words = std::min(g.tile_words, room);
     if (b->direction == 0 && g.tile_words > room / 2) {   // global slots for tiles that outgrow the staging
-      g.gimg_words = (size_t)persistent_grid() * 2 * g.tile_words;
+      g.gimg_words = (size_t)persistent_grid() * 2 * slot_stride(g.tile_words);
       if ((e = cudaMalloc((void**)&g.gimg, g.gimg_words * 8)) != cudaSuccess) {
         fail_cuda("zfp_gb300_batch_create: staging", e);
         destroy(b);

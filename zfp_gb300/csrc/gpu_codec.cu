@@ -385,8 +385,8 @@ static cudaError_t plan_launch(LaunchArgs& a, int type, int dims, bool encode, u
   a.img_words = (uint32_t)std::min<uint64_t>(words, room);
   if (encode && words > room) {
     a.grid = (int)std::min<uint64_t>(total_tiles, (uint64_t)persistent_grid());
-    a.slot_words = (uint32_t)words;
-    cudaError_t e = gimg.alloc((size_t)a.grid * words * 8, st);
+    a.slot_words = slot_stride(words);
+    cudaError_t e = gimg.alloc((size_t)a.grid * a.slot_words * 8, st);
     if (e != cudaSuccess) return e;
     a.gimg = (uint64_t*)gimg.p;
   }

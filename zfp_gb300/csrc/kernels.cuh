@@ -391,8 +391,9 @@ __device__ __forceinline__ void write_tile(const Job& job, const LaunchScratch& 
 // The tile image lives in shared memory (`simg`, `img_words` words) when the
 // tile's code fits there, else in this CTA's slot of global memory (`gslot`,
 // `slot_words` words, sized for the largest possible tile).
+// returns the words of the global slot the tile's image used (0: it was in shared memory)
 template <typename S, int D, int kSel>
-__device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch& sc, uint32_t gt, uint64_t* simg,
+__device__ __forceinline__ uint32_t encode_tile(const Job& job, const LaunchScratch& sc, uint32_t gt, uint64_t* simg,
                                             uint32_t img_words, uint64_t* gslot, uint32_t slot_words,
                                             uint64_t* planes, const uint32_t* gtab) {
   using B = typename Traits<S>::Bits;
@@ -464,6 +465,16 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
   write_tile(job, sc, lt, gt, img, nw, G, total);
   if (active && (job.flags & kWriteIndex)) job.offsets[b] = G + excl;
   if (threadIdx.x == 0 && lt + 1 == job.ntiles) job.result->end_bit = G + total;
+  return in_smem || !nw ? 0u : img_phys(nw - 1) + 1;
+}
+
+// Once a tile image in a global slot has been copied to the stream its data
+// is dead: drop its L2 lines instead of letting them be written back to
+// DRAM (slots are whole 128-byte lines, one per CTA, so no other CTA's data
+// shares them).  Called by the whole CTA after the reads of the image.
+__device__ __forceinline__ void discard_slot(uint64_t* slot, uint32_t words) {
+  for (uint32_t l = threadIdx.x; l < (words + 15) / 16; l += kTile)
+    asm volatile("discard.global.L2 [%0], 128;" ::"l"(__cvta_generic_to_global(slot + 16 * (size_t)l)) : "memory");
 }
 
 // dynamic shared memory for the bit planes of one tile (1-3D blocks)
@@ -615,8 +626,9 @@ __device__ __forceinline__ void encode_body(const Job& one, const Job* jobs, int
     const uint32_t gt = s_tile;
     if (gt >= total_tiles) break;
     const Job* job = resolve_job<kMulti>(one, jobs, njobs, gt, &s_job);
-    encode_tile<S, D, kSel>(*job, sc, gt, smem_img, img_words, gslot, slot_words, planes, s_gtab);
+    const uint32_t used = encode_tile<S, D, kSel>(*job, sc, gt, smem_img, img_words, gslot, slot_words, planes, s_gtab);
     __syncthreads();
+    if (used) discard_slot(gslot, used);
   }
 }
 

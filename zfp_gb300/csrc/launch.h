@@ -35,6 +35,11 @@ template <typename S, int D> cudaError_t run_parse(const Job& job, cudaStream_t 
 // occupancy.
 template <typename S, int D> uint32_t stage_room(const LaunchArgs& a, bool encode);
 
+// Stride of the encoder's per-CTA global image slots: whole 128-byte lines,
+// so a tile can drop its slot's lines from L2 once they are read (the
+// kernels' discard of dead slot data)
+inline uint32_t slot_stride(uint64_t words) { return (uint32_t)((words + 15) & ~(uint64_t)15); }
+
 // 64-bit words of storage for `logical` words of tile image or staged stream:
 // the kernels keep a spare word after every 16 (shared-memory bank spreading)
 inline uint64_t image_words(uint64_t logical) { return logical + logical / 16 + 1; }

@@ -176,9 +176,9 @@ static cudaError_t launch_batch(Server* s, Lane* lane) {
       a.img_words = std::min(g.img_words, room);
       if (r.direction == 0 && g.img_words > room) {   // tiles larger than shared memory: one global slot per CTA
         a.grid = (int)std::min<uint64_t>(g.tiles, (uint64_t)persistent_grid());
-        a.slot_words = g.img_words;
+        a.slot_words = slot_stride(g.img_words);
         g.gimg_off = off;
-        g.gimg_bytes = (size_t)a.grid * g.img_words * 8;
+        g.gimg_bytes = (size_t)a.grid * a.slot_words * 8;
         off += (g.gimg_bytes + 255) & ~(size_t)255;
       }
     }
