@@ -136,6 +136,19 @@ int zfp_gb300_server_stats(zfp_gb300_server* server, size_t* peak_bytes, uint64_
 /* Finish everything submitted, stop the dispatcher and release the server. */
 void zfp_gb300_server_free(zfp_gb300_server* server);
 
+/* ---- many blocks per call: zfp's block codec in one launch ---------------
+ * No counterpart in the reference, which codes one block per call
+ * (zfp_encode_block_* / zfp_decode_block_*, declared in zfp.h and also
+ * provided here).  `count` full 4^d blocks stored one after another (4^d
+ * values each, x fastest) are coded in one GPU launch at the stream's
+ * current bit, bit for bit as `count` successive zfp_encode_block_<type>_<dims>
+ * calls would write them (and read back as `count` zfp_decode_block calls
+ * would): the stream is left at the exact end bit, not flushed.  Blocks and
+ * stream may be host or device memory.  Returns the bits written / read, 0
+ * on failure. */
+size_t zfp_gb300_encode_blocks(zfp_stream* zfp, zfp_type type, unsigned int dims, const void* blocks, size_t count);
+size_t zfp_gb300_decode_blocks(zfp_stream* zfp, zfp_type type, unsigned int dims, void* blocks, size_t count);
+
 /* ---- compression without device allocation -----------------------------
  * No counterpart in the reference: zfp_compress there has no GPU scratch.
  * Same stream as zfp_compress (zfp_exec_cuda), for callers that cannot let

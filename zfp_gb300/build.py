@@ -16,7 +16,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 CFLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-O3"]
 
-SOURCES = ["zfp_api.cpp", "gpu_codec.cu", "batch.cu", "noalloc.cu", "serve.cu", "index.cu"] + [f"kern_{t}_{d}d.cu" for t in ("f32", "f64", "i32", "i64") for d in (1, 2, 3, 4)]
+SOURCES = ["zfp_api.cpp", "blocks.cpp", "gpu_codec.cu", "batch.cu", "noalloc.cu", "serve.cu", "index.cu"] + [f"kern_{t}_{d}d.cu" for t in ("f32", "f64", "i32", "i64") for d in (1, 2, 3, 4)]
 
 
 def _deps() -> list[str]:

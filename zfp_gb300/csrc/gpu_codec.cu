@@ -466,7 +466,7 @@ struct LaunchMem {
 // ---------------------------------------------------------------------------
 // compress
 
-size_t gpu_compress(zfp_stream* z, const zfp_field* f) {
+size_t gpu_compress(zfp_stream* z, const zfp_field* f, bool exact_end, uint64_t* bits_out) {
   ExecParams* ep = exec_params(z);
   if (!ep) return fail("zfp_compress: stream has no GPU execution parameters");
   if (!z->stream) return fail("zfp_compress: no bit stream");
@@ -551,7 +551,7 @@ size_t gpu_compress(zfp_stream* z, const zfp_field* f) {
       (e = launch_encode_any(fi.type, fi.dims, a, st)) != cudaSuccess)
     return fail_cuda("zfp_compress: launch", e);
 
-  if (fixed && field_dev && stream_dev && ep->async) {
+  if (fixed && field_dev && stream_dev && ep->async && !exact_end) {
     const uint64_t end = bit0 + fi.nblocks * (uint64_t)z->maxbits;
     registry_invalidate(ss.begin, bit0, end);
     set_stream_flushed(z->stream, end);
@@ -580,7 +580,12 @@ size_t gpu_compress(zfp_stream* z, const zfp_field* f) {
   } else {
     registry_invalidate(ss.begin, bit0, end);
   }
-  set_stream_flushed(z->stream, end);
+  if (exact_end) {
+    if (!set_stream_written(z->stream, end, stream_dev)) return fail("zfp_compress: reading the stream's last word");
+  } else {
+    set_stream_flushed(z->stream, end);
+  }
+  if (bits_out) *bits_out = end - bit0;
   set_error("");
   return (size_t)((end + 63) / 64) * 8;
 }
@@ -588,7 +593,7 @@ size_t gpu_compress(zfp_stream* z, const zfp_field* f) {
 // ---------------------------------------------------------------------------
 // decompress
 
-size_t gpu_decompress(zfp_stream* z, zfp_field* f) {
+size_t gpu_decompress(zfp_stream* z, zfp_field* f, bool exact_end, uint64_t* bits_out) {
   ExecParams* ep = exec_params(z);
   if (!ep) return fail("zfp_decompress: stream has no GPU execution parameters");
   if (!z->stream) return fail("zfp_decompress: no bit stream");
@@ -719,7 +724,7 @@ size_t gpu_decompress(zfp_stream* z, zfp_field* f) {
   a.one = job;
   if ((e = launch_decode_any(fi.type, fi.dims, a, st)) != cudaSuccess) return fail_cuda("zfp_decompress: launch", e);
 
-  const bool async_ok = fixed && field_dev && stream_dev && ep->async;
+  const bool async_ok = fixed && field_dev && stream_dev && ep->async && !exact_end;
   if (!async_ok) {
     JobResult res;
     if ((e = cudaMemcpyAsync(&res, lm.result, sizeof res, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
@@ -742,7 +747,12 @@ size_t gpu_decompress(zfp_stream* z, zfp_field* f) {
     g_staged += span;
   }
   if (parsed) registry_insert(make_entry(ss.begin, bit0, end, fi, job, parsed));
-  set_stream_flushed(z->stream, end);
+  if (exact_end) {
+    if (!set_stream_read_at(z->stream, end, stream_dev)) return fail("zfp_decompress: reading the stream's last word");
+  } else {
+    set_stream_flushed(z->stream, end);
+  }
+  if (bits_out) *bits_out = end - bit0;
   set_error("");
   return (size_t)((end + 63) / 64) * 8;
 }

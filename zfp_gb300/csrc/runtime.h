@@ -27,7 +27,17 @@ void set_error(const char* msg);
 bool ensure_exec_params(zfp_stream* z);
 void release_exec_params(zfp_stream* z);
 
-size_t gpu_compress(zfp_stream* z, const zfp_field* f);
-size_t gpu_decompress(zfp_stream* z, zfp_field* f);
+// exact_end: leave the stream at the exact end bit instead of flushed /
+// aligned (the reference's block functions do: stream_pad / stream_align is
+// the caller's); bits_out receives the bits coded
+size_t gpu_compress(zfp_stream* z, const zfp_field* f, bool exact_end = false, uint64_t* bits_out = nullptr);
+size_t gpu_decompress(zfp_stream* z, zfp_field* f, bool exact_end = false, uint64_t* bits_out = nullptr);
+
+// the reference's writer state after writing up to end_bit without a flush:
+// the last partial word's bits held in `buffer` (read back from the stream's
+// memory, which the GPU already wrote; device memory if `device`)
+bool set_stream_written(bitstream* s, uint64_t end_bit, bool device);
+// the reader state of stream_rseek(end_bit): the rest of the current word in `buffer`
+bool set_stream_read_at(bitstream* s, uint64_t end_bit, bool device);
 
 }  // namespace zg

@@ -720,4 +720,44 @@ void set_stream_flushed(bitstream* s, uint64_t end_bit) {
   s->buffer = 0;
 }
 
+static bool read_word(const uint64_t* p, bool device, uint64_t& w) {
+  if (!device) {
+    w = *p;
+    return true;
+  }
+  if (cudaMemcpy(&w, p, sizeof w, cudaMemcpyDeviceToHost) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return true;
+}
+
+// writer state (include/zfp/bitstream.inl:133-143): `bits` buffered bits in
+// `buffer`, ptr at the word they will go to
+bool set_stream_written(bitstream* s, uint64_t end_bit, bool device) {
+  s->ptr = s->begin + end_bit / 64;
+  s->bits = end_bit % 64;
+  s->buffer = 0;
+  if (!s->bits) return true;
+  uint64_t w;
+  if (!read_word(s->ptr, device, w)) return false;
+  s->buffer = w & ((uint64_t(1) << s->bits) - 1);
+  return true;
+}
+
+// reader state of stream_rseek (include/zfp/bitstream.inl:340-352)
+bool set_stream_read_at(bitstream* s, uint64_t end_bit, bool device) {
+  const unsigned n = (unsigned)(end_bit % 64);
+  s->ptr = s->begin + end_bit / 64;
+  s->buffer = 0;
+  s->bits = 0;
+  if (!n) return true;
+  uint64_t w;
+  if (!read_word(s->ptr, device, w)) return false;
+  s->ptr++;
+  s->buffer = w >> n;
+  s->bits = 64 - n;
+  return true;
+}
+
 }  // namespace zg
