@@ -249,6 +249,49 @@ struct SmemSink {
   }
 };
 
+// Sink of a fixed-rate block that starts and ends on a stream word: no
+// other block shares its words, so it writes them straight to the stream
+// (padding included: the stream is not zeroed beforehand).  `room` counts
+// the stream words from `out` on; stores past them are dropped and flagged.
+struct StreamSink {
+  uint64_t* out;
+  uint64_t room;
+  uint64_t word;
+  unsigned fill;
+  uint64_t acc;
+  unsigned* status;
+
+  __device__ __forceinline__ void store(uint64_t w) {
+    if (word < room) out[word] = w;
+    else atomicOr(status, (unsigned)kStatusOverflow);
+    word++;
+  }
+  // v must have no bits at or above n
+  __device__ __forceinline__ void put(uint64_t v, unsigned n) {
+    acc |= v << fill;
+    const unsigned t = fill + n;
+    if (t >= 64) {
+      store(acc);
+      acc = fill ? v >> (64 - fill) : 0;
+      fill = t - 64;
+    } else {
+      fill = t;
+    }
+  }
+  __device__ __forceinline__ void pad(unsigned n) {
+    unsigned t = fill + n;
+    while (t >= 64) {
+      store(acc);
+      acc = 0;
+      t -= 64;
+    }
+    fill = t;
+  }
+  __device__ __forceinline__ void finish() {
+    if (fill) store(acc);
+  }
+};
+
 // ---------------------------------------------------------------------------
 // CTA-wide exclusive scan of one value per thread
 
@@ -406,6 +449,8 @@ __device__ __forceinline__ uint32_t encode_tile(const Job& job, const LaunchScra
   const uint64_t b = (uint64_t)lt * kTile + threadIdx.x;
   const bool active = b < job.nblocks;
   const bool fixed = job.flags & kFixedRate;
+  // fixed-rate blocks on word boundaries go straight to the stream (no image)
+  const bool direct = fixed && !((job.maxbits | job.bit0) & 63u);
   const BlockParams p{job.minbits, job.maxbits, job.maxprec, job.minexp};
   uint64_t* my_planes = planes + threadIdx.x;   // plane k of this block at my_planes[k * kTile]
 
@@ -433,7 +478,7 @@ __device__ __forceinline__ uint32_t encode_tile(const Job& job, const LaunchScra
   const uint32_t need = (total + 63) / 64 + 1;
   const bool in_smem = need <= img_cap(img_words) || !gslot;
   uint64_t* img = in_smem ? simg : gslot;
-  const uint32_t nw = min(need, img_cap(in_smem ? img_words : slot_words));
+  const uint32_t nw = direct ? 0u : min(need, img_cap(in_smem ? img_words : slot_words));
   for (uint32_t i = threadIdx.x; i < nw; i += kTile) img[img_phys(i)] = 0;
   if (threadIdx.x == 0) {
     if (fixed) s_base = (unsigned long long)lt * kTile * job.maxbits;
@@ -441,7 +486,13 @@ __device__ __forceinline__ uint32_t encode_tile(const Job& job, const LaunchScra
   }
   __syncthreads();
 
-  if (active) {
+  if (active && direct) {
+    const uint64_t w0 = job.bit0 / 64 + b * (job.maxbits / 64);
+    StreamSink out{job.words + w0, job.cap_words > w0 ? job.cap_words - w0 : 0, 0, 0, 0ull, &job.result->status};
+    if constexpr (N <= 64) emit_block_seq<P, N>(out, h, my_planes, kTile, gtab);
+    else wc.emit(out, gtab);
+    out.finish();
+  } else if (active) {
     if constexpr (N <= 64) {
       SmemSink out{img, excl >> 6, excl & 63u, 0ull, true, nw, &job.result->status};
       emit_block_seq<P, N>(out, h, my_planes, kTile, gtab);
@@ -462,7 +513,7 @@ __device__ __forceinline__ uint32_t encode_tile(const Job& job, const LaunchScra
   __syncthreads();
 
   const uint64_t G = job.bit0 + s_base;
-  write_tile(job, sc, lt, gt, img, nw, G, total);
+  if (!direct) write_tile(job, sc, lt, gt, img, nw, G, total);
   if (active && (job.flags & kWriteIndex)) job.offsets[b] = G + excl;
   if (threadIdx.x == 0 && lt + 1 == job.ntiles) job.result->end_bit = G + total;
   return in_smem || !nw ? 0u : img_phys(nw - 1) + 1;
