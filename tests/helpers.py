@@ -73,12 +73,16 @@ def zfp_run(lib, direction, data_ptr, ztype, n, s, mode, arg, buf_ptr, buf_bytes
         lib.stream_close(bs)
 
 
-def oracle_stream(oracle, view, mode, arg, prefix=None):
-    """Oracle stream words for a numpy view (with the same prefix bits)."""
+def oracle_stream(oracle, view, mode, arg, prefix=None, room=0):
+    """Oracle stream words for a numpy view (with the same prefix bits).
+    `room`: words to provide at least, for budgets below the block header
+    size, where the reference's bit budget wraps around and blocks run past
+    what zfp_stream_maximum_size allows for."""
     n, s = geometry(view)
     prm = mode_params(mode, arg, view.dtype, len(n))
     bit0 = 0
-    words = np.zeros(oracle.max_words(n, view.dtype, prm) + 8 + (prefix[0] if prefix else 0), dtype=np.uint64)
+    words = np.zeros(max(room, oracle.max_words(n, view.dtype, prm)) + 8 + (prefix[0] if prefix else 0),
+                     dtype=np.uint64)
     if prefix:
         word, value, nbits = prefix
         bit0 = 64 * word + nbits

@@ -83,12 +83,12 @@ class DevSpan:
 
 
 def run_case(lib, oracle, torch, dtype, shape, mode, arg, layout="c", field_dev=False, stream_dev=False,
-             prefix=None, kind="smooth", async_=False):
+             prefix=None, kind="smooth", async_=False, room=0):
     base = make_values(dtype, base_shape(shape, layout), kind)
     view = make_view(base, layout)
     n, s = geometry(view)
     zt = ztype_of(view)
-    exp_words, exp_end, prm = oracle_stream(oracle, view, mode, arg, prefix)
+    exp_words, exp_end, prm = oracle_stream(oracle, view, mode, arg, prefix, room)
     nwords = len(exp_words) + 16
 
     fspan = DevSpan(torch, view) if field_dev else None
@@ -190,6 +190,25 @@ def test_many_tiles(lib, oracle, cuda):
         run_case(lib, oracle, cuda, np.float64, (40, 64, 90), mode, arg, field_dev=True, stream_dev=True,
                  prefix=(0, 0x3, 2))
         run_case(lib, oracle, cuda, np.float32, (257, 129), mode, arg, layout="perm")
+
+
+@pytest.mark.parametrize("dtype", DTYPES, ids=lambda d: np.dtype(d).name)
+def test_tiny_budgets(lib, oracle, cuda, dtype):
+    """Expert-mode budgets of a few bits per block over many tiles, streams
+    starting on and off a word: integer blocks of no bits at all (maxbits 0)
+    leave only the bits ahead of the stream; a float budget below the block
+    header makes the reference's remaining budget wrap around, so its blocks
+    code in full (zfp_stream_maximum_size does not hold for them)."""
+    shape = (40, 64, 90)
+    room = 10 * 16 * 23 * (64 * 65 + 64) // 64
+    params = [(0, 0, 64, -1074), (0, 1, 64, -1074), (1, 1, 64, -1074), (0, 3, 1, -1074), (2, 2, 64, -1074),
+              (0, 9, 64, -1074), (12, 12, 64, -1074), (0, 20, 3, 0)]
+    for prm in params:
+        if np.dtype(dtype).kind == "f" and prm[1] < 1:
+            continue   # a float block codes at least one bit
+        for prefix in (None, (1, 0x2b, 7), (0, 0x5, 3)):
+            run_case(lib, oracle, cuda, dtype, shape, "expert", prm, prefix=prefix, room=room)
+        run_case(lib, oracle, cuda, dtype, shape, "expert", prm, field_dev=True, stream_dev=True, room=room)
 
 
 def test_async_fixed_rate(lib, oracle, cuda):

@@ -402,30 +402,39 @@ __device__ __forceinline__ void write_tile(const Job& job, const LaunchScratch& 
   const uint64_t hw = G >> 6, tw = E >> 6;
   const unsigned sh = (unsigned)(G & 63), te = (unsigned)(E & 63);
   const bool first = lt == 0, last = lt + 1 == job.ntiles;
+  // A tile codes no bits only when every block of the job does (maxbits 0):
+  // then nothing but the caller's bits ahead of the stream goes out.
+  if (!total) {
+    if (first && sh && threadIdx.x == 0) store_word(job, hw, job.head_word & ((1ull << sh) - 1));
+    return;
+  }
   const uint32_t cnt = (uint32_t)((te ? tw + 1 : tw) - hw);   // stream words this tile touches
   const bool in_bounds = hw + cnt <= job.cap_words;
-  const unsigned lane = threadIdx.x & 31;
-  // whole warps step through the words so the word below comes from the
-  // neighbouring lane; lane 0 reads its own
-  for (uint32_t base = threadIdx.x - lane; base < cnt; base += kTile) {
-    const uint32_t j = base + lane;
+  // stream word hw + j: image word j shifted up by sh, with the top of word j - 1 below
+  auto word = [&](uint32_t j) -> uint64_t {
     const uint64_t cur = j < nimg ? img[img_phys(j)] : 0ull;
-    uint64_t prev = __shfl_up_sync(0xffffffffu, cur, 1);
-    if (lane == 0) prev = j && j - 1 < nimg ? img[img_phys(j - 1)] : 0ull;
-    if (j >= cnt) continue;
-    uint64_t v = sh ? (cur << sh) | (prev >> (64 - sh)) : cur;
-    const uint64_t w = hw + j;
-    if (j == 0 && sh) {
-      if (first) v |= job.head_word & ((1ull << sh) - 1);
-      else {
-        merge_word(job, sc, gt, 1, w, v);
-        continue;
-      }
-    }
-    if (w == tw && te && !last) merge_word(job, sc, gt + 1, 0, w, v);
-    else if (in_bounds) job.words[w] = v;
-    else store_word(job, w, v);
+    if (!sh) return cur;
+    const uint64_t prev = j && j - 1 < nimg ? img[img_phys(j - 1)] : 0ull;
+    return (cur << sh) | (prev >> (64 - sh));
+  };
+  // a tile that does not start (end) on a word shares its first (last) word
+  // with the previous (next) tile of the job; every word in between is its
+  // own.  Otherwise every block codes at least one bit, a tile other than a
+  // job's last holds at least 128 bits, and those two shared words are
+  // distinct.
+  const uint32_t jlo = sh ? 1u : 0u;
+  const uint32_t jhi = te && !last ? cnt - 1 : cnt;
+  for (uint32_t j = jlo + threadIdx.x; j < jhi; j += kTile) {
+    const uint64_t v = word(j);
+    if (in_bounds) job.words[hw + j] = v;
+    else store_word(job, hw + j, v);
   }
+  if (threadIdx.x == 0 && sh) {
+    const uint64_t v = word(0);
+    if (first) store_word(job, hw, v | (job.head_word & ((1ull << sh) - 1)));
+    else merge_word(job, sc, gt, 1, hw, v);
+  }
+  if (threadIdx.x == kTile - 1 && te && !last) merge_word(job, sc, gt + 1, 0, tw, word(cnt - 1));
 }
 
 // ---------------------------------------------------------------------------
