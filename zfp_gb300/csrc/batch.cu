@@ -38,8 +38,6 @@ struct BatchGroup {
   LaunchScratch sc{};
   void* scratch = nullptr;     // zeroed before every launch
   size_t scratch_bytes = 0;
-  uint64_t* gimg = nullptr;    // encode: global slots for tiles larger than img_words
-  size_t gimg_words = 0;
 };
 
 }  // namespace zg
@@ -81,20 +79,14 @@ static cudaError_t enqueue(zfp_gb300_batch* b, cudaStream_t st, int ctas_per_sm,
     a.sc = g.sc;
     a.total_tiles = g.total_tiles;
     a.use_ticket = 1;
-    // less staging only where the tiles it no longer holds have somewhere
-    // to go: the decoder reads them from the stream, the encoder needs its
-    // global slots
+    // tiles the staging no longer holds are read from the stream (decode)
+    // or coded straight into it (encode)
     a.img_words = g.img_words;
-    if (stage_pct < 100 && (b->direction == 1 || g.gimg))
+    if (stage_pct < 100)
       a.img_words = std::max<uint32_t>(std::min<uint32_t>(64, g.img_words),
                                        (uint32_t)((uint64_t)g.img_words * stage_pct / 100));
     const int grid = std::max(1, sm_count() * ctas_per_sm);
     a.grid = (int)std::min<uint64_t>(g.total_tiles, (uint64_t)grid);
-    if (g.gimg && g.tile_words > a.img_words) {
-      a.gimg = g.gimg;
-      a.slot_words = slot_stride(g.tile_words);
-      a.grid = (int)std::min<uint64_t>((uint64_t)a.grid, g.gimg_words / a.slot_words);
-    }
     e = b->direction == 0 ? launch_encode_any(g.type, g.dims, a, st) : launch_decode_any(g.type, g.dims, a, st);
     if (e != cudaSuccess) return e;
   }
@@ -108,7 +100,6 @@ static void destroy(zfp_gb300_batch* b) {
   for (auto& g : b->groups) {
     cudaFree(g.d_jobs);
     cudaFree(g.scratch);
-    cudaFree(g.gimg);
   }
   cudaFree(b->d_results);
   cudaFree(b->d_offsets);
@@ -267,14 +258,6 @@ zfp_gb300_batch* zfp_gb300_batch_create(zfp_stream* const* streams, const zfp_fi
     probe.jobs = g.d_jobs;
     const uint32_t room = stage_room_any(g.type, g.dims, probe, b->direction == 0);
     g.img_words = std::min(g.tile_words, room);
-    if (b->direction == 0 && g.tile_words > room / 2) {   // global slots for tiles that outgrow the staging
-      g.gimg_words = (size_t)persistent_grid() * 2 * slot_stride(g.tile_words);
-      if ((e = cudaMalloc((void**)&g.gimg, g.gimg_words * 8)) != cudaSuccess) {
-        fail_cuda("zfp_gb300_batch_create: staging", e);
-        destroy(b);
-        return nullptr;
-      }
-    }
   }
   set_error("");
   return b;

@@ -367,30 +367,19 @@ int persistent_grid() {
   return sms * 4;
 }
 
-// decide shared- or global-memory staging and the grid
 // Launch geometry; a.one / a.jobs must be set (they select the kernel).
 // `bound_bits` bounds one block's code, so a tile's image never exceeds
-// `words`.  Encode: the image lives in shared memory up to the kernel's
-// occupancy room; when a tile may be larger, a persistent grid gets one
-// global slot per CTA for such tiles.  Decode: up to the room of a tile's
-// stream words is staged; larger tiles are read from the stream directly.
-static cudaError_t plan_launch(LaunchArgs& a, int type, int dims, bool encode, uint64_t bound_bits,
-                               uint32_t total_tiles, DevBuf& gimg, cudaStream_t st) {
+// `words`.  Up to the kernel's occupancy room the tile's image (encode) or
+// stream words (decode) are staged in shared memory; larger tiles are coded
+// straight into the stream, or read from it directly.  A fixed-rate encode
+// stages nothing: its tiles' places are known without the look-back.
+static void plan_launch(LaunchArgs& a, int type, int dims, bool encode, uint64_t bound_bits, uint32_t total_tiles) {
   const uint64_t words = image_words((uint64_t)kTile * bound_bits / 64 + 4);
-  const uint32_t room = stage_room_any(type, dims, a, encode);
+  const bool fixed_encode = encode && !a.jobs && (a.one.flags & kFixedRate);
+  const uint32_t room = fixed_encode ? 0 : stage_room_any(type, dims, a, encode);
   a.total_tiles = total_tiles;
   a.grid = (int)total_tiles;
-  a.gimg = nullptr;
-  a.slot_words = 0;
   a.img_words = (uint32_t)std::min<uint64_t>(words, room);
-  if (encode && words > room) {
-    a.grid = (int)std::min<uint64_t>(total_tiles, (uint64_t)persistent_grid());
-    a.slot_words = slot_stride(words);
-    cudaError_t e = gimg.alloc((size_t)a.grid * a.slot_words * 8, st);
-    if (e != cudaSuccess) return e;
-    a.gimg = (uint64_t*)gimg.p;
-  }
-  return cudaSuccess;
 }
 
 template <class F>
@@ -545,11 +534,8 @@ size_t gpu_compress(zfp_stream* z, const zfp_field* f, bool exact_end, uint64_t*
   a.njobs = 1;
   a.sc = lm.sc;
   a.use_ticket = fixed ? 0 : 1;
-  DevBuf gimg;
-  if ((e = plan_launch(a, fi.type, fi.dims, true, fixed ? z->maxbits : bound, job.ntiles, gimg, st)) !=
-          cudaSuccess ||
-      (e = launch_encode_any(fi.type, fi.dims, a, st)) != cudaSuccess)
-    return fail_cuda("zfp_compress: launch", e);
+  plan_launch(a, fi.type, fi.dims, true, fixed ? z->maxbits : bound, job.ntiles);
+  if ((e = launch_encode_any(fi.type, fi.dims, a, st)) != cudaSuccess) return fail_cuda("zfp_compress: launch", e);
 
   if (fixed && field_dev && stream_dev && ep->async && !exact_end) {
     const uint64_t end = bit0 + fi.nblocks * (uint64_t)z->maxbits;
@@ -717,10 +703,7 @@ size_t gpu_decompress(zfp_stream* z, zfp_field* f, bool exact_end, uint64_t* bit
   a.sc = lm.sc;
   a.one = job;
   a.want_words = want_words;
-  DevBuf gimg;
-  if ((e = plan_launch(a, fi.type, fi.dims, false, fixed ? z->maxbits : bound, job.ntiles, gimg, st)) !=
-      cudaSuccess)
-    return fail_cuda("zfp_decompress: plan", e);
+  plan_launch(a, fi.type, fi.dims, false, fixed ? z->maxbits : bound, job.ntiles);
   a.one = job;
   if ((e = launch_decode_any(fi.type, fi.dims, a, st)) != cudaSuccess) return fail_cuda("zfp_decompress: launch", e);
 

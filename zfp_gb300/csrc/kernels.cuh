@@ -292,6 +292,66 @@ struct StreamSink {
   }
 };
 
+// One block written straight into the stream from bit `fill` of word
+// `dst` on; the caller has checked that the block's words lie inside the
+// stream buffer.  Words the block covers whole are stored; its first word,
+// when it starts inside it, and its last word, when it ends inside it, hold
+// bits of the neighbouring blocks too: those are OR-ed into the tile's seam
+// table (shared memory, entries at shared addresses `head` and `tail`) and
+// stored once every block of the tile has added its part.
+constexpr uint32_t kNoSeam = ~0u;
+
+// (no "memory" clobber: the barrier after the tile's blocks orders these
+// with the reads of the table, and the coder's loads of its bit planes stay
+// free to be scheduled around them)
+__device__ __forceinline__ void seam_or(uint32_t addr, uint64_t v) {
+  asm volatile("red.shared.or.b64 [%0], %1;" ::"r"(addr), "l"(v));
+}
+
+struct SeamSink {
+  uint64_t* dst;
+  unsigned fill;
+  uint64_t acc;
+  uint32_t head;      // kNoSeam when the block starts on a word
+  uint32_t tail;
+
+  __device__ __forceinline__ void store(uint64_t w) {
+    if (head != kNoSeam) {
+      seam_or(head, w);
+      head = kNoSeam;
+    } else {
+      *dst = w;
+    }
+    dst++;
+  }
+  // v must have no bits at or above n
+  __device__ __forceinline__ void put(uint64_t v, unsigned n) {
+    acc |= v << fill;
+    const unsigned t = fill + n;
+    if (t >= 64) {
+      store(acc);
+      acc = fill ? v >> (64 - fill) : 0;
+      fill = t - 64;
+    } else {
+      fill = t;
+    }
+  }
+  __device__ __forceinline__ void pad(unsigned n) {
+    unsigned t = fill + n;
+    while (t >= 64) {
+      store(acc);
+      acc = 0;
+      t -= 64;
+    }
+    fill = t;
+  }
+  // a block ending inside the word that it starts inside has the same entry
+  // for both
+  __device__ __forceinline__ void finish() {
+    if (fill) seam_or(tail, acc);
+  }
+};
+
 // ---------------------------------------------------------------------------
 // CTA-wide exclusive scan of one value per thread
 
@@ -440,28 +500,46 @@ __device__ __forceinline__ void write_tile(const Job& job, const LaunchScratch& 
 // ---------------------------------------------------------------------------
 // encode one tile
 
-// The tile image lives in shared memory (`simg`, `img_words` words) when the
-// tile's code fits there, else in this CTA's slot of global memory (`gslot`,
-// `slot_words` words, sized for the largest possible tile).
-// returns the words of the global slot the tile's image used (0: it was in shared memory)
+// Bit planes first (with each block's length, for variable rates), then the
+// tile's place in the stream: its first bit G follows from the tile number
+// at a fixed rate, else from the decoupled look-back.
+//
+// A variable-rate tile whose code fits the shared-memory image (`img`,
+// `img_words` words) is coded there while the look-back runs, and copied
+// out at G by write_tile: the look-back's wait for the tiles before it
+// overlaps the coding.
+//
+// Every other tile -- fixed-rate ones, whose G needs no look-back, and
+// variable-rate ones too large for the image -- is coded straight into the
+// stream (SeamSink).  Boundary i of the tile (block i's first bit; boundary
+// nb is the tile's end) lies in stream word W_i; a word holding a boundary
+// inside it is shared, and its seam entry is that of the first boundary in
+// the word.  Blocks of 64 bits or more put every boundary in a word of its
+// own; shorter ones (zero blocks of the lossy modes) can put several in
+// one, found through the table of the boundaries' words.  The first and
+// last words of the tile may be shared with the neighbouring tiles of the
+// job: those go through merge_word.
 template <typename S, int D, int kSel>
-__device__ __forceinline__ uint32_t encode_tile(const Job& job, const LaunchScratch& sc, uint32_t gt, uint64_t* simg,
-                                            uint32_t img_words, uint64_t* gslot, uint32_t slot_words,
-                                            uint64_t* planes, const uint32_t* gtab) {
+__device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch& sc, uint32_t gt, uint64_t* img,
+                                            uint32_t img_words, uint64_t* planes, const uint32_t* gtab) {
   using B = typename Traits<S>::Bits;
   using U = typename Traits<S>::UInt;
   constexpr int N = 1 << (2 * D);
   constexpr int P = 8 * sizeof(U);
   __shared__ uint32_t s_warp[kTile / 32];
   __shared__ unsigned long long s_base;
+  __shared__ unsigned long long s_seam[kTile + 1];
+  __shared__ uint32_t s_word[kTile + 1];   // W_i - W_0, when a tile has blocks under 64 bits
   const uint32_t lt = gt - job.tile0;
-  const uint64_t b = (uint64_t)lt * kTile + threadIdx.x;
+  const uint32_t bi = threadIdx.x;
+  const uint64_t b = (uint64_t)lt * kTile + bi;
   const bool active = b < job.nblocks;
+  const uint64_t left = job.nblocks - (uint64_t)lt * kTile;
+  const uint32_t nb = left < kTile ? (uint32_t)left : kTile;
   const bool fixed = job.flags & kFixedRate;
-  // fixed-rate blocks on word boundaries go straight to the stream (no image)
-  const bool direct = fixed && !((job.maxbits | job.bit0) & 63u);
+  const bool first = lt == 0, last = lt + 1 == job.ntiles;
   const BlockParams p{job.minbits, job.maxbits, job.maxprec, job.minexp};
-  uint64_t* my_planes = planes + threadIdx.x;   // plane k of this block at my_planes[k * kTile]
+  uint64_t* my_planes = planes + bi;   // plane k of this block at my_planes[k * kTile]
 
   uint32_t len = 0;
   BlockHead h;
@@ -483,58 +561,103 @@ __device__ __forceinline__ uint32_t encode_tile(const Job& job, const LaunchScra
   }
   uint32_t total;
   const uint32_t excl = cta_exclusive_scan(len, total, s_warp);
-
-  const uint32_t need = (total + 63) / 64 + 1;
-  const bool in_smem = need <= img_cap(img_words) || !gslot;
-  uint64_t* img = in_smem ? simg : gslot;
-  const uint32_t nw = direct ? 0u : min(need, img_cap(in_smem ? img_words : slot_words));
-  for (uint32_t i = threadIdx.x; i < nw; i += kTile) img[img_phys(i)] = 0;
-  if (threadIdx.x == 0) {
+  if (bi == 0) {
     if (fixed) s_base = (unsigned long long)lt * kTile * job.maxbits;
     else publish_aggregate(job, sc, gt, total);
   }
-  __syncthreads();
 
-  if (active && direct) {
-    const uint64_t w0 = job.bit0 / 64 + b * (job.maxbits / 64);
-    StreamSink out{job.words + w0, job.cap_words > w0 ? job.cap_words - w0 : 0, 0, 0, 0ull, &job.result->status};
-    if constexpr (N <= 64) emit_block_seq<P, N>(out, h, my_planes, kTile, gtab);
-    else wc.emit(out, gtab);
-    out.finish();
-  } else if (active) {
-    if constexpr (N <= 64) {
+  const uint32_t need = (total + 63) / 64 + 1;
+  // The fixed-precision kernel is launched only where the image holds the
+  // largest possible tile (see with_encoder), so it is built with this path
+  // alone: measured 6% faster at precision 20 than with both paths.
+  constexpr bool kStagedOnly = kSel == kLossyFloor;
+  if (kStagedOnly || (!fixed && total && need <= img_cap(img_words))) {
+    const uint32_t nw = kStagedOnly ? min(need, img_cap(img_words)) : need;   // stores past it are flagged
+    for (uint32_t i = bi; i < nw; i += kTile) img[img_phys(i)] = 0;
+    __syncthreads();
+    if (active) {
       SmemSink out{img, excl >> 6, excl & 63u, 0ull, true, nw, &job.result->status};
-      emit_block_seq<P, N>(out, h, my_planes, kTile, gtab);
-      out.finish();
-    } else {
-      SmemSink out{img, excl >> 6, excl & 63u, 0ull, true, nw, &job.result->status};
-      wc.emit(out, gtab);
+      if constexpr (N <= 64) emit_block_seq<P, N>(out, h, my_planes, kTile, gtab);
+      else wc.emit(out, gtab);
       out.finish();
     }
+    // the last warp resolves the tile's place after its own blocks, by when
+    // the tiles before have mostly published theirs
+    if (bi >= kTile - 32) {
+      const uint64_t before = look_back(job, sc, gt, total);
+      if (bi == kTile - 32) s_base = before;
+    }
+    __syncthreads();
+    const uint64_t G = job.bit0 + s_base;
+    write_tile(job, sc, lt, gt, img, nw, G, total);
+    if (active && (job.flags & kWriteIndex)) job.offsets[b] = G + excl;
+    if (bi == 0 && last) job.result->end_bit = G + total;
+    return;
   }
-  // the tile's place in the stream is needed only by write_tile: the last
-  // warp resolves it after its own blocks, by when the predecessors have
-  // mostly published theirs
-  if (!fixed && threadIdx.x >= kTile - 32) {
+
+  s_seam[bi] = 0;
+  if (bi == 0) s_seam[kTile] = 0;
+  if (!fixed && bi >= kTile - 32) {
     const uint64_t before = look_back(job, sc, gt, total);
-    if (threadIdx.x == kTile - 32) s_base = before;
+    if (bi == kTile - 32) s_base = before;
+  }
+  const bool small = __syncthreads_or(active && len < 64);
+
+  const uint64_t G = job.bit0 + s_base, E = G + total;
+  const uint64_t pos = G + excl, end = pos + len;
+  if (active && (job.flags & kWriteIndex)) job.offsets[b] = pos;
+  if (bi == 0 && last) job.result->end_bit = E;
+  // A block codes no bits only when every block of the job does (maxbits
+  // 0): then nothing but the caller's bits ahead of the stream goes out.
+  // Otherwise every block has a bit at least.
+  if (!total) {
+    if (bi == 0 && first && (G & 63)) store_word(job, G >> 6, job.head_word & ((1ull << (G & 63)) - 1));
+    return;
+  }
+  // seam entries of this block's boundaries (its first bit and its end)
+  uint32_t lo = bi, hi = bi + 1;
+  if (small) {
+    const uint64_t w0 = G >> 6;
+    if (active) s_word[bi] = (uint32_t)((pos >> 6) - w0);
+    if (bi + 1 == nb) s_word[nb] = (uint32_t)((E >> 6) - w0);
+    __syncthreads();
+    if (active) {
+      const uint32_t w = s_word[bi];
+      while (lo && s_word[lo - 1] == w) lo--;
+      hi = s_word[bi + 1] == w ? lo : bi + 1;
+    }
+  }
+
+  if (active) {
+    if ((end + 63) >> 6 <= job.cap_words) {
+      const uint32_t seam0 = (uint32_t)__cvta_generic_to_shared(s_seam);
+      SeamSink out{job.words + (pos >> 6), (unsigned)(pos & 63), 0ull, (pos & 63) ? seam0 + 8 * lo : kNoSeam,
+                   seam0 + 8 * hi};
+      if constexpr (N <= 64) emit_block_seq<P, N>(out, h, my_planes, kTile, gtab);
+      else wc.emit(out, gtab);
+      out.finish();
+    } else {
+      atomicOr(&job.result->status, (unsigned)kStatusOverflow);
+    }
   }
   __syncthreads();
 
-  const uint64_t G = job.bit0 + s_base;
-  if (!direct) write_tile(job, sc, lt, gt, img, nw, G, total);
-  if (active && (job.flags & kWriteIndex)) job.offsets[b] = G + excl;
-  if (threadIdx.x == 0 && lt + 1 == job.ntiles) job.result->end_bit = G + total;
-  return in_smem || !nw ? 0u : img_phys(nw - 1) + 1;
-}
-
-// Once a tile image in a global slot has been copied to the stream its data
-// is dead: drop its L2 lines instead of letting them be written back to
-// DRAM (slots are whole 128-byte lines, one per CTA, so no other CTA's data
-// shares them).  Called by the whole CTA after the reads of the image.
-__device__ __forceinline__ void discard_slot(uint64_t* slot, uint32_t words) {
-  for (uint32_t l = threadIdx.x; l < (words + 15) / 16; l += kTile)
-    asm volatile("discard.global.L2 [%0], 128;" ::"l"(__cvta_generic_to_global(slot + 16 * (size_t)l)) : "memory");
+  // shared words out: each by the first boundary in it
+  auto seam_out = [&](uint32_t i, uint64_t w, uint64_t v) {
+    const unsigned sh = (unsigned)(G & 63);
+    if (i == 0 && sh) {
+      if (first) store_word(job, w, v | (job.head_word & ((1ull << sh) - 1)));
+      else merge_word(job, sc, gt, 1, w, v);
+    } else if (w == (E >> 6) && (E & 63) && !last) {
+      merge_word(job, sc, gt + 1, 0, w, v);
+    } else {
+      store_word(job, w, v);
+    }
+  };
+  if (active) {
+    if (lo == bi && ((pos & 63) || hi == lo)) seam_out(bi, pos >> 6, s_seam[bi]);
+    if (bi + 1 == nb && hi == nb && (end & 63)) seam_out(nb, end >> 6, s_seam[nb]);
+  }
 }
 
 // dynamic shared memory for the bit planes of one tile (1-3D blocks)
@@ -671,10 +794,8 @@ __device__ __forceinline__ const Job* resolve_job(const Job& one, const Job* job
 
 template <typename S, int D, bool kMulti, int kSel>
 __device__ __forceinline__ void encode_body(const Job& one, const Job* jobs, int njobs, const LaunchScratch& sc,
-                                            uint32_t total_tiles, int use_ticket, uint64_t* gimg,
-                                            uint32_t slot_words, uint32_t img_words) {
+                                            uint32_t total_tiles, int use_ticket, uint32_t img_words) {
   extern __shared__ uint64_t smem_img[];
-  uint64_t* gslot = gimg ? gimg + (size_t)blockIdx.x * slot_words : nullptr;
   uint64_t* planes = plane_base<S, D, kMulti, kSel>(smem_img + img_words, one);
   __shared__ uint32_t s_tile;
   __shared__ Job s_job;
@@ -686,26 +807,24 @@ __device__ __forceinline__ void encode_body(const Job& one, const Job* jobs, int
     const uint32_t gt = s_tile;
     if (gt >= total_tiles) break;
     const Job* job = resolve_job<kMulti>(one, jobs, njobs, gt, &s_job);
-    const uint32_t used = encode_tile<S, D, kSel>(*job, sc, gt, smem_img, img_words, gslot, slot_words, planes, s_gtab);
+    encode_tile<S, D, kSel>(*job, sc, gt, smem_img, img_words, planes, s_gtab);
     __syncthreads();
-    if (used) discard_slot(gslot, used);
   }
 }
 
 template <typename S, int D, bool kMulti, int kSel>
 __global__ void __launch_bounds__(kTile) encode_kernel(const __grid_constant__ Job one, const Job* jobs, int njobs,
                                                        LaunchScratch sc, uint32_t total_tiles, int use_ticket,
-                                                       uint64_t* gimg, uint32_t slot_words, uint32_t img_words) {
-  encode_body<S, D, kMulti, kSel>(one, jobs, njobs, sc, total_tiles, use_ticket, gimg, slot_words, img_words);
+                                                       uint32_t img_words) {
+  encode_body<S, D, kMulti, kSel>(one, jobs, njobs, sc, total_tiles, use_ticket, img_words);
 }
 
 // The same encoder held to more CTAs per SM (see decode_kernel_occ).
 template <typename S, int D, bool kMulti, int kSel, int kMinCtas>
 __global__ void __launch_bounds__(kTile, kMinCtas) encode_kernel_occ(const __grid_constant__ Job one, const Job* jobs,
                                                                      int njobs, LaunchScratch sc, uint32_t total_tiles,
-                                                                     int use_ticket, uint64_t* gimg,
-                                                                     uint32_t slot_words, uint32_t img_words) {
-  encode_body<S, D, kMulti, kSel>(one, jobs, njobs, sc, total_tiles, use_ticket, gimg, slot_words, img_words);
+                                                                     int use_ticket, uint32_t img_words) {
+  encode_body<S, D, kMulti, kSel>(one, jobs, njobs, sc, total_tiles, use_ticket, img_words);
 }
 
 // img_words: shared memory for staging a tile's stream words; tiles that do

@@ -16,8 +16,6 @@ struct LaunchArgs {
   uint32_t total_tiles;
   int use_ticket;
   uint32_t img_words;     // shared-memory words per CTA for the tile image / staged stream words
-  uint64_t* gimg;         // encode: one slot of slot_words per CTA for tiles larger than img_words
-  uint32_t slot_words;
   int grid;
   uint32_t want_words;    // decode planning: stream words a typical tile stages (0: unknown)
 };
@@ -35,17 +33,12 @@ template <typename S, int D> cudaError_t run_parse(const Job& job, cudaStream_t 
 // occupancy.
 template <typename S, int D> uint32_t stage_room(const LaunchArgs& a, bool encode);
 
-// Stride of the encoder's per-CTA global image slots: whole 128-byte lines,
-// so a tile can drop its slot's lines from L2 once they are read (the
-// kernels' discard of dead slot data)
-inline uint32_t slot_stride(uint64_t words) { return (uint32_t)((words + 15) & ~(uint64_t)15); }
-
 // 64-bit words of storage for `logical` words of tile image or staged stream:
 // the kernels keep a spare word after every 16 (shared-memory bank spreading)
 inline uint64_t image_words(uint64_t logical) { return logical + logical / 16 + 1; }
 
-// a tile image plus bit planes larger than this is staged in global memory
-// instead (GB300 allows 227 KB of shared memory per CTA, static included)
+// shared memory a CTA may take for its tile image or staged stream words
+// beside its bit planes (GB300 allows 227 KB per CTA, static included)
 constexpr size_t kMaxTileSmem = 216 * 1024;
 
 // shared memory the kernels keep for bit planes: 1-3D blocks only

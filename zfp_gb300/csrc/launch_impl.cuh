@@ -103,20 +103,41 @@ static bool five_ctas(const Job& j) {
   }
 }
 
+// bits of one block of a 32-bit fixed-precision job at most (block_bound):
+// the header and every coded plane
+template <typename S, int D>
+static uint64_t floor_block_bound(const Job& j) {
+  constexpr uint64_t N = 1u << (2 * D), hm = std::is_floating_point<S>::value ? 1 + 8 : 0;
+  uint64_t b = hm + N - 1 + N * (uint64_t)j.maxprec;
+  if (j.maxbits >= hm) b = std::min<uint64_t>(b, j.maxbits);
+  return std::max<uint64_t>(b, j.minbits);
+}
+
 template <typename S, int D>
 static bool five_ctas_floor(const Job& j) {
   if constexpr (sizeof(S) != 4 || D > 3) {
     return false;
   } else {
-    // bits of one block at most (block_bound): the header and every coded plane
-    constexpr uint64_t N = 1u << (2 * D), P = 32, hm = std::is_floating_point<S>::value ? 1 + 8 : 0;
-    if ((j.flags & kFixedRate) || j.maxprec >= P) return false;
-    uint64_t b = hm + N - 1 + N * (uint64_t)j.maxprec;
-    if (j.maxbits >= hm) b = std::min<uint64_t>(b, j.maxbits);
-    b = std::max<uint64_t>(b, j.minbits);
-    const size_t tile =
-        image_words((uint64_t)kTile * b / 64 + 4) * 8 + plane_smem_bytes<S, D, false, true>(false, j.maxprec);
+    if ((j.flags & kFixedRate) || j.maxprec >= 32) return false;
+    const size_t tile = image_words((uint64_t)kTile * floor_block_bound<S, D>(j) / 64 + 4) * 8 +
+                        plane_smem_bytes<S, D, false, true>(false, j.maxprec);
     return tile <= kFifthShare;
+  }
+}
+
+// The fixed-precision encoder stages every tile whole in shared memory (it
+// is built without the path that codes straight into the stream), so it is
+// chosen only where the largest possible tile fits the room its occupancy
+// leaves -- computed from the kernel's own attributes, the same way for
+// planning and for launching.
+template <typename S, int D>
+static bool floor_encoder_fits(const Job& j) {
+  if constexpr (sizeof(S) != 4 || D > 3) {
+    return false;
+  } else {
+    const uint64_t words = image_words((uint64_t)kTile * floor_block_bound<S, D>(j) / 64 + 4);
+    const size_t planes = plane_smem_bytes<S, D, true, true>(false, j.maxprec);
+    return words * 8 <= smem_room<encode_kernel_occ<S, D, false, kLossyFloor, 5>>(planes);
   }
 }
 
@@ -128,7 +149,8 @@ static auto with_encoder(const LaunchArgs& a, F&& f) {
     else return f(KernelTag<encode_kernel<S, D, false, kRevOnly>>{});
   }
   if constexpr (sizeof(S) == 4 && D <= 3) {
-    if (five_ctas_floor<S, D>(a.one)) return f(KernelTag<encode_kernel_occ<S, D, false, kLossyFloor, 5>, true>{});
+    if (five_ctas_floor<S, D>(a.one) && floor_encoder_fits<S, D>(a.one))
+      return f(KernelTag<encode_kernel_occ<S, D, false, kLossyFloor, 5>, true>{});
     if (five_ctas<S, D>(a.one)) return f(KernelTag<encode_kernel_occ<S, D, false, kLossyOnly, 5>>{});
     if constexpr (D == 3) return f(KernelTag<encode_kernel_occ<S, D, false, kLossyOnly, 4>>{});
   }
@@ -175,8 +197,7 @@ cudaError_t run_encode(const LaunchArgs& a, cudaStream_t st) {
     constexpr auto kernel = decltype(tag)::kernel;
     const size_t smem = (size_t)a.img_words * 8 + planes_of<S, D, true, decltype(tag)>(a);
     prepare_kernel<kernel>();
-    kernel<<<a.grid, kTile, smem, st>>>(a.one, a.jobs, a.njobs, a.sc, a.total_tiles, a.use_ticket, a.gimg,
-                                        a.slot_words, a.img_words);
+    kernel<<<a.grid, kTile, smem, st>>>(a.one, a.jobs, a.njobs, a.sc, a.total_tiles, a.use_ticket, a.img_words);
     return cudaGetLastError();
   });
 }

@@ -21,6 +21,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 
@@ -103,9 +104,6 @@ extern "C" size_t zfp_gb300_compress_noalloc(zfp_stream* z, const zfp_field* f) 
     return fail("zfp_gb300_compress_noalloc: field has more than 4194304 blocks (the scratch limit)");
   const bool fixed = is_fixed_rate(fi, z);
   const uint64_t bound = fixed ? (uint64_t)z->maxbits : block_bound(fi, z);
-  const uint64_t img_words = image_words((uint64_t)kTile * bound / 64 + 4);
-  if (img_words * 8 + plane_bytes(fi.esize, fi.dims) > kMaxTileSmem)
-    return fail("zfp_gb300_compress_noalloc: blocks too large for shared-memory staging");
   const uint64_t bit0 = (uint64_t)(ss.ptr - ss.begin) * 64 + ss.bits;
   const uint64_t cap_words = (uint64_t)(ss.end - ss.begin);
   if (fixed && (bit0 + fi.nblocks * (uint64_t)z->maxbits + 63) / 64 > cap_words)
@@ -140,7 +138,11 @@ extern "C" size_t zfp_gb300_compress_noalloc(zfp_stream* z, const zfp_field* f) 
   a.sc.wait_cycles = wait_cycles();
   a.total_tiles = (uint32_t)ntiles;
   a.use_ticket = fixed ? 0 : 1;
-  a.img_words = (uint32_t)img_words;
+  // variable-rate tiles are staged in shared memory up to the kernel's
+  // occupancy room, larger ones coded straight into the stream
+  a.img_words = fixed ? 0u
+                      : (uint32_t)std::min<uint64_t>(image_words((uint64_t)kTile * bound / 64 + 4),
+                                                     stage_room_any(fi.type, fi.dims, a, true));
   a.grid = (int)ntiles;
   if ((e = launch_encode_any(fi.type, fi.dims, a, st)) != cudaSuccess)
     return fail_cuda("zfp_gb300_compress_noalloc: launch", e);

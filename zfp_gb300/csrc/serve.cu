@@ -136,7 +136,7 @@ static cudaError_t launch_batch(Server* s, Lane* lane) {
   // device layout: results | per group: jobs, scratch | block indexes
   size_t off = ((reqs.size() * sizeof(JobResult)) + 255) & ~(size_t)255;
   struct G { int type, dims; std::vector<size_t> idx; uint32_t tiles = 0, img_words = 0; size_t jobs_off, scr_off,
-             scr_bytes; LaunchArgs one; size_t gimg_off = 0, gimg_bytes = 0; };
+             scr_bytes; LaunchArgs one; };
   std::vector<G> gs;
   for (auto& kv : groups) {
     G g;
@@ -172,15 +172,9 @@ static cudaError_t launch_batch(Server* s, Lane* lane) {
         const uint64_t end = r.fixed ? r.nominal_end : r.job.end_bit;
         a.want_words = (uint32_t)std::min<uint64_t>(image_words((end - r.job.bit0) / g.tiles / 64 + 4), 1u << 30);
       }
-      const uint32_t room = stage_room_any(g.type, g.dims, a, r.direction == 0);
+      const bool fixed_encode = r.direction == 0 && r.fixed;   // places known without the look-back
+      const uint32_t room = fixed_encode ? 0 : stage_room_any(g.type, g.dims, a, r.direction == 0);
       a.img_words = std::min(g.img_words, room);
-      if (r.direction == 0 && g.img_words > room) {   // tiles larger than shared memory: one global slot per CTA
-        a.grid = (int)std::min<uint64_t>(g.tiles, (uint64_t)persistent_grid());
-        a.slot_words = slot_stride(g.img_words);
-        g.gimg_off = off;
-        g.gimg_bytes = (size_t)a.grid * a.slot_words * 8;
-        off += (g.gimg_bytes + 255) & ~(size_t)255;
-      }
     }
     gs.push_back(g);
   }
@@ -213,14 +207,11 @@ static cudaError_t launch_batch(Server* s, Lane* lane) {
         (e = cudaMemsetAsync(base + g.scr_off, 0, g.scr_bytes, lane->st)) != cudaSuccess)
       return e;
     const Request& r0 = *reqs[g.idx[0]];
-    const size_t planes = plane_bytes(r0.fi.esize, g.dims);
-    if ((size_t)g.img_words * 8 + planes > kMaxTileSmem) return cudaErrorInvalidValue;  // refused at submit
     const bool single = g.idx.size() == 1;
     LaunchArgs a;
     if (single) {
       a = g.one;
       a.one = lane->host_jobs[hj - 1];   // with its result and index pointers
-      if (g.gimg_bytes) a.gimg = (uint64_t*)(base + g.gimg_off);
     } else {
       std::memset(&a, 0, sizeof a);
       a.one = r0.job;
@@ -238,9 +229,9 @@ static cudaError_t launch_batch(Server* s, Lane* lane) {
     const bool enc = reqs[g.idx[0]]->direction == 0;
     if (!single) {
       a.use_ticket = 1;
-      // encode keeps whole tile images in shared memory (no global slots);
-      // decode stages only what fits the kernel's occupancy room
-      a.img_words = enc ? g.img_words : std::min(g.img_words, stage_room_any(g.type, g.dims, a, false));
+      // tiles larger than the kernel's occupancy room are coded straight
+      // into the stream (encode) or read from it directly (decode)
+      a.img_words = std::min(g.img_words, stage_room_any(g.type, g.dims, a, enc));
       a.grid = (int)std::min<uint64_t>(g.tiles, (uint64_t)persistent_grid());
     }
     e = enc ? launch_encode_any(g.type, g.dims, a, lane->st) : launch_decode_any(g.type, g.dims, a, lane->st);
@@ -413,11 +404,6 @@ uint64_t zfp_gb300_server_submit(zfp_gb300_server* s, zfp_stream* z, const zfp_f
   }
   const FieldInfo& fi = r->fi;
   r->fixed = is_fixed_rate(fi, z);
-  const uint64_t bound = r->fixed ? (uint64_t)z->maxbits : block_bound(fi, z);
-  if (image_words((uint64_t)kTile * bound / 64 + 4) * 8 + plane_bytes(fi.esize, fi.dims) > kMaxTileSmem) {
-    fail("zfp_gb300_server_submit: blocks too large for shared-memory staging");
-    return 0;
-  }
   Job j = base_job(fi, z, f->data);
   j.flags = (r->fixed ? kFixedRate : 0u) | vector_flags(fi, f->data);
   j.words = ss.begin;
