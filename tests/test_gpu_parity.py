@@ -35,9 +35,14 @@ def make_values(dtype, shape, kind="smooth"):
         x = np.cumsum(RNG.standard_normal(shape), axis=-1)
         if len(shape) > 1:
             x = np.cumsum(x, axis=0)
+        if kind == "patchy":   # runs of two zero blocks between runs of two coded ones
+            x[..., (np.arange(shape[-1]) // 8) % 2 == 0] = 0
         return (x * 10.0 ** RNG.uniform(-4, 4)).astype(dtype)
     bits = 28 if dtype == np.int32 else 58
-    return np.cumsum(RNG.integers(-(1 << 20), 1 << 20, size=shape), axis=-1).clip(-(1 << bits), 1 << bits).astype(dtype)
+    x = np.cumsum(RNG.integers(-(1 << 20), 1 << 20, size=shape), axis=-1).clip(-(1 << bits), 1 << bits)
+    if kind == "patchy":
+        x[..., (np.arange(shape[-1]) // 8) % 2 == 0] = 0
+    return x.astype(dtype)
 
 
 def make_view(base, layout):
@@ -190,6 +195,21 @@ def test_many_tiles(lib, oracle, cuda):
         run_case(lib, oracle, cuda, np.float64, (40, 64, 90), mode, arg, field_dev=True, stream_dev=True,
                  prefix=(0, 0x3, 2))
         run_case(lib, oracle, cuda, np.float32, (257, 129), mode, arg, layout="perm")
+
+
+@pytest.mark.parametrize("dtype,mode,arg", [(np.float64, "accuracy", 1e-3), (np.float64, "reversible", None),
+                                            (np.float64, "precision", 40), (np.float32, "accuracy", 1e-6),
+                                            (np.float32, "precision", 32), (np.int64, "reversible", None)],
+                         ids=lambda v: str(v))
+def test_direct_tiles_with_short_blocks(lib, oracle, cuda, dtype, mode, arg):
+    """Tiles too large for the encoder's shared-memory image are coded
+    straight into the stream.  Zero blocks code in a bit or a few, so several
+    block boundaries share one stream word; they alternate here with coded
+    blocks over many tiles, on and off word boundaries, host and device."""
+    shape = (40, 64, 90)
+    for prefix in (None, (1, 0x2b, 7), (0, 0x5, 3)):
+        run_case(lib, oracle, cuda, dtype, shape, mode, arg, prefix=prefix, kind="patchy")
+    run_case(lib, oracle, cuda, dtype, shape, mode, arg, field_dev=True, stream_dev=True, kind="patchy")
 
 
 @pytest.mark.parametrize("dtype", DTYPES, ids=lambda d: np.dtype(d).name)
