@@ -310,7 +310,9 @@ def gpu_arm(args):
     key = f"{dom['field']}_{dom['mode']}_{dom['dir']}"
     roofline = {"bound": "hbm", "kernel": key, "achieved": round(dom["hbm_gbs"], 1), "peak": peak,
                 "peak_kind": peak_kind, "unit": "GB/s", "frac": round(dom["hbm_gbs"] / peak, 4),
-                "traffic": traffic.get(key)}
+                "traffic": traffic.get(key),
+                "traffic_source": "profiles/traffic.txt: an earlier ncu capture of this kernel on the same field "
+                                  "(dram__bytes_read.sum + dram__bytes_write.sum), not measured in this run"}
     fixed = [r for r in per if r["mode"] == "rate"]
 
     # the reference's own CUDA backend on the same fields (fixed rate 8)
