@@ -347,6 +347,31 @@ def test_pinned_host_buffers_zero_copy(lib, oracle, cuda):
         assert np.array_equal(out2.view(np.uint8), ref_out.view(np.uint8)), msg
 
 
+def test_pinned_stream_offsets(lib, oracle, cuda):
+    """Page-locked streams starting inside a word, written in place: tiles are
+    staged in shared memory (fixed rate too) and the caller's bits ahead of
+    the stream survive."""
+    torch = cuda
+    for dtype, shape, mode, arg in [(np.float32, (40, 64, 90), "rate", 8), (np.float32, (40, 64, 90), "rate", 5.5),
+                                    (np.float64, (33, 40, 50), "accuracy", 1e-3),
+                                    (np.float64, (33, 40, 50), "reversible", None)]:
+        vals = make_values(dtype, shape)
+        for prefix in ((1, 0x2b, 7), (0, 0x5, 3)):
+            exp_words, _, prm = oracle_stream(oracle, vals, mode, arg, prefix)
+            nwords = len(exp_words) + 16
+            hs = torch.zeros(nwords, dtype=torch.int64, pin_memory=True)
+            hx = torch.from_numpy(vals.copy()).pin_memory()
+            n, s = geometry(vals)
+            r, _ = zfp_run(lib, "compress", hx.data_ptr(), ztype_of(vals), n, s, mode, arg, hs.data_ptr(),
+                           nwords * 8, prefix)
+            msg = f"{np.dtype(dtype).name} {shape} {mode}={arg} prefix={prefix}"
+            assert r == len(exp_words) * 8, (msg, lib.zfp_gb300_last_error())
+            assert lib.zfp_gb300_last_staged_bytes() == 0, msg
+            got = hs.numpy().view(np.uint64)[: len(exp_words)]
+            bad = np.nonzero(got != exp_words)[0]
+            assert bad.size == 0, (msg, bad[:8])
+
+
 def test_pinned_stream_uploaded_when_tiles_exceed_shared_memory(lib, oracle, cuda):
     """A page-locked stream whose decode tiles do not fit the decoder's shared
     memory (2D 64-bit reversible noise: about 19 KB a tile beside 64 KB of

@@ -372,11 +372,19 @@ int persistent_grid() {
 // `words`.  Up to the kernel's occupancy room the tile's image (encode) or
 // stream words (decode) are staged in shared memory; larger tiles are coded
 // straight into the stream, or read from it directly.  A fixed-rate encode
-// stages nothing: its tiles' places are known without the look-back.
+// stages nothing: its tiles' places are known without the look-back.  An
+// encode into host memory (written in place over the host link, which only
+// whole lines cross at speed) stages whole tiles wherever shared memory
+// holds them, at the cost of CTAs per SM: such a call is bound by the link.
 static void plan_launch(LaunchArgs& a, int type, int dims, bool encode, uint64_t bound_bits, uint32_t total_tiles) {
   const uint64_t words = image_words((uint64_t)kTile * bound_bits / 64 + 4);
   const bool fixed_encode = encode && !a.jobs && (a.one.flags & kFixedRate);
-  const uint32_t room = fixed_encode ? 0 : stage_room_any(type, dims, a, encode);
+  const bool host_encode = encode && !a.jobs && (a.one.flags & kStreamHost);
+  const size_t esize = type == zfp_type_float || type == zfp_type_int32 ? 4 : 8;
+  const size_t planes = plane_bytes(esize, dims);   // at most what the kernel keeps
+  const uint32_t room = host_encode ? (uint32_t)((kMaxTileSmem > planes ? kMaxTileSmem - planes : 0) / 8)
+                        : fixed_encode ? 0
+                                       : stage_room_any(type, dims, a, encode);
   a.total_tiles = total_tiles;
   a.grid = (int)total_tiles;
   a.img_words = (uint32_t)std::min<uint64_t>(words, room);
@@ -506,7 +514,7 @@ size_t gpu_compress(zfp_stream* z, const zfp_field* f, bool exact_end, uint64_t*
   }
 
   Job job = base_job(fi, z, dfield);
-  job.flags = (fixed ? kFixedRate : 0u) | vector_flags(fi, dfield);
+  job.flags = (fixed ? kFixedRate : 0u) | (stream_map ? kStreamHost : 0u) | vector_flags(fi, dfield);
   job.words = dwords;
   job.cap_words = dcap;
   job.bit0 = bit0;

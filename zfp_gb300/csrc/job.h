@@ -18,6 +18,9 @@ enum JobFlags : uint32_t {
   kWriteIndex = 4u,  // encode: record each block's start bit in `offsets`
   kVerify = 8u,      // decode: check every block ends where the next begins
   kVec32 = 16u,      // with kVecOk, 64-bit rows (32 bytes) are 32-byte aligned: one access per row
+  kStreamHost = 32u, // encode: the stream is host memory written in place over the host link, where
+                     // only whole coalesced lines go at speed: tiles are staged in shared memory
+                     // (fixed rate too) whenever they fit
 };
 
 enum JobStatus : uint32_t {

@@ -571,7 +571,8 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
   // largest possible tile (see with_encoder), so it is built with this path
   // alone: measured 6% faster at precision 20 than with both paths.
   constexpr bool kStagedOnly = kSel == kLossyFloor;
-  if (kStagedOnly || (!fixed && total && need <= img_cap(img_words))) {
+  const bool stage = !fixed || (job.flags & kStreamHost);
+  if (kStagedOnly || (stage && total && need <= img_cap(img_words))) {
     const uint32_t nw = kStagedOnly ? min(need, img_cap(img_words)) : need;   // stores past it are flagged
     for (uint32_t i = bi; i < nw; i += kTile) img[img_phys(i)] = 0;
     __syncthreads();
@@ -583,7 +584,7 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
     }
     // the last warp resolves the tile's place after its own blocks, by when
     // the tiles before have mostly published theirs
-    if (bi >= kTile - 32) {
+    if (!fixed && bi >= kTile - 32) {
       const uint64_t before = look_back(job, sc, gt, total);
       if (bi == kTile - 32) s_base = before;
     }
