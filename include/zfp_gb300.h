@@ -157,9 +157,8 @@ size_t zfp_gb300_decode_blocks(zfp_stream* zfp, zfp_type type, unsigned int dims
  * not trigger an allocation.  Field and stream buffers must be in device
  * memory; nothing is staged, and the encoder's scratch is a fixed 1 MiB
  * device array inside the library (held by every GPU that loads it), which
- * limits a call to 4,194,304 zfp blocks (e.g. 512^3 float) and to blocks
- * whose tile fits shared memory.  Larger or host-resident inputs return 0
- * with a reason in zfp_gb300_last_error().  The first call on a device (in
+ * limits a call to 4,194,304 zfp blocks (e.g. 512^3 float).  Larger or
+ * host-resident inputs return 0 with a reason in zfp_gb300_last_error().  The first call on a device (in
  * each CUDA context of it) does a set-up step: it looks up that array's
  * device address.  Make that first call before any CUDA stream capture
  * begins.  Each call waits for its own GPU work before it returns.  All

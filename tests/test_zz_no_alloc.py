@@ -47,6 +47,8 @@ CASES = [  # shape (numpy order), dtype, mode, arg, prefix bits
     ((17, 29, 23), np.float32, "precision", 16, 11),
     ((300, 257), np.float64, "rate", 12.5, 5),
     ((64, 64, 64, 8), np.float32, "accuracy", 1e-2, 0),
+    # 4D 64-bit reversible: tiles far larger than shared memory, coded straight into the stream
+    ((12, 10, 9, 11), np.float64, "reversible", None, 3),
 ]
 
 
