@@ -332,7 +332,14 @@ def gpu_arm(args):
     e2e = None
     if not args.no_e2e:
         e2e = e2e_run(lib, torch, codec, fields, args)
-        e2e["host_link"] = host_link(torch)
+        link = e2e["host_link"] = host_link(torch)
+        # each call against the link: its bytes at the copy engines' one-way
+        # rates, overlapped, and at their rate both ways at once
+        for c in e2e["per_call"]:
+            one_way = max(c["h2d_bytes"] / link["h2d_gbs"], c["d2h_bytes"] / link["d2h_gbs"]) / 1e6
+            both = (c["h2d_bytes"] + c["d2h_bytes"]) / link["bidirectional_gbs"] / 1e6
+            c["link_bound_ms"] = round(max(one_way, both), 3)
+            c["frac_of_link"] = round(c["link_bound_ms"] / c["ms"], 3) if c["ms"] else None
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -795,24 +802,31 @@ def e2e_run(lib, torch, codec, fields, args):
     h2d = d2h = 0
     sizes = {}
     staged = [0]
+    calls = {}   # (field, mode, direction) -> fastest call in seconds (the calls are synchronous)
+
+    def call(fd, direction, ptr, mode, arg, hbuf):
+        t0 = time.perf_counter()
+        r = codec.run(direction, ptr, fd["ztype"], fd["n"], mode, arg, hbuf.data_ptr(), fd["cap"], async_=False)
+        dt = time.perf_counter() - t0
+        key = (fd["name"], mode, direction)
+        calls[key] = min(calls.get(key, 1e30), dt)
+        staged[0] += lib.zfp_gb300_last_staged_bytes()
+        return r
 
     def step():
         staged[0] = 0
         for fd, hx, hout, hbuf in hosts:
             for mode, arg in MODES:
-                r = codec.run("c", hx.data_ptr(), fd["ztype"], fd["n"], mode, arg, hbuf.data_ptr(), fd["cap"],
-                              async_=False)
-                staged[0] += lib.zfp_gb300_last_staged_bytes()
-                r2 = codec.run("d", hout.data_ptr(), fd["ztype"], fd["n"], mode, arg, hbuf.data_ptr(), fd["cap"],
-                               async_=False)
-                staged[0] += lib.zfp_gb300_last_staged_bytes()
+                r = call(fd, "c", hx.data_ptr(), mode, arg, hbuf)
+                r2 = call(fd, "d", hout.data_ptr(), mode, arg, hbuf)
                 if not r or r2 != r:
                     raise RuntimeError(f"e2e {fd['name']} {mode} failed")
                 sizes[(fd["name"], mode)] = r
 
     step()
     torch.cuda.synchronize()
-    n = max(1, min(args.steps, 3))
+    calls.clear()
+    n = max(1, min(args.steps, 10))
     t0 = time.perf_counter()
     for _ in range(n):
         step()
@@ -824,8 +838,17 @@ def e2e_run(lib, torch, codec, fields, args):
             h2d += fd["raw"] + sizes[(fd["name"], mode)]
             d2h += fd["raw"] + sizes[(fd["name"], mode)]
     _, world, _ = dist_info()
+    per_call = []
+    for fd in fields:
+        for mode, _ in MODES:
+            size = sizes[(fd["name"], mode)]
+            for direction in ("c", "d"):
+                per_call.append({"field": fd["name"], "mode": mode, "dir": direction,
+                                 "ms": round(calls[(fd["name"], mode, direction)] * 1e3, 3),
+                                 "h2d_bytes": fd["raw"] if direction == "c" else size,
+                                 "d2h_bytes": size if direction == "c" else fd["raw"]})
     return {"value": round(world * raw_step * n / dt / 1e9, 2), "unit": "GB/s", "h2d_bytes_per_step": h2d,
-            "d2h_bytes_per_step": d2h, "steps": n,
+            "d2h_bytes_per_step": d2h, "steps": n, "per_call": per_call,
             "buffers": "pinned host field and stream, read and written in place by the kernels over the host link, "
                        "except streams whose decode tiles outgrow shared memory, uploaded once (staged_bytes_per_step); "
                        "h2d/d2h = bytes crossing the link", "staged_bytes_per_step": staged[0]}
