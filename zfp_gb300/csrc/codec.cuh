@@ -545,16 +545,49 @@ ZG_HD void lift(I& a, I& b, I& c, I& d) {
 }
 
 template <LiftKind K, int D, typename I>
+ZG_HD void xform(I (&v)[1 << (2 * D)]);
+
+// 4D: lifts along x, y and z never mix the four w-slices of 64 values, so
+// each slice goes through the 3D transform in registers (all of its
+// indexes compile-time), and the w lifts -- one per (x, y, z) position
+// across the slices -- come after (forward) or before (inverse) them.  The
+// block array itself stays in local memory; only whole slices and one
+// position's four values cross it.
+template <LiftKind K, typename I>
+ZG_HD void xform4(I (&v)[256]) {
+  constexpr bool kInverse = (K == kInv || K == kRevInv);
+  auto w_lifts = [&]() {
+#pragma unroll 4
+    for (int j = 0; j < 64; j++) lift<K>(v[j], v[j + 64], v[j + 128], v[j + 192]);
+  };
+  if (kInverse) w_lifts();
+#pragma unroll 1
+  for (int w = 0; w < 4; w++) {
+    I r[64];
+#pragma unroll
+    for (int j = 0; j < 64; j++) r[j] = v[64 * w + j];
+    xform<K, 3>(r);
+#pragma unroll
+    for (int j = 0; j < 64; j++) v[64 * w + j] = r[j];
+  }
+  if (!kInverse) w_lifts();
+}
+
+template <LiftKind K, int D, typename I>
 ZG_HD void xform(I (&v)[1 << (2 * D)]) {
   constexpr int N = 1 << (2 * D);
   constexpr bool kInverse = (K == kInv || K == kRevInv);
+  if constexpr (D == 4) {
+    xform4<K>(v);
+  } else {
 #pragma unroll
-  for (int step = 0; step < D; step++) {
-    const int axis = kInverse ? D - 1 - step : step;
-    const int s = 1 << (2 * axis);
-#pragma unroll (N <= 64 ? N : 1)
-    for (int i = 0; i < N; i++)
-      if (((i >> (2 * axis)) & 3) == 0) lift<K>(v[i], v[i + s], v[i + 2 * s], v[i + 3 * s]);
+    for (int step = 0; step < D; step++) {
+      const int axis = kInverse ? D - 1 - step : step;
+      const int s = 1 << (2 * axis);
+#pragma unroll
+      for (int i = 0; i < N; i++)
+        if (((i >> (2 * axis)) & 3) == 0) lift<K>(v[i], v[i + s], v[i + 2 * s], v[i + 3 * s]);
+    }
   }
 }
 
