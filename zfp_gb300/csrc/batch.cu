@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <utility>
 #include <vector>
 
@@ -33,6 +34,7 @@ struct BatchGroup {
   uint32_t total_tiles = 0;
   uint32_t tile_words = 0;     // largest tile image of any member
   uint32_t img_words = 0;      // shared-memory part at full staging (see plan_launch in gpu_codec.cu)
+  bool lossy = true;           // no member is reversible: the lossy-only multi-job kernels
   bool needs_ticket = false;
   Job* d_jobs = nullptr;       // device copy of this group's jobs (sorted by tile0)
   LaunchScratch sc{};
@@ -76,6 +78,7 @@ static cudaError_t enqueue(zfp_gb300_batch* b, cudaStream_t st, int ctas_per_sm,
     a.one = b->jobs[g.members[0]];
     a.jobs = g.d_jobs;
     a.njobs = (int)g.members.size();
+    a.multi_lossy = g.lossy;
     a.sc = g.sc;
     a.total_tiles = g.total_tiles;
     a.use_ticket = 1;
@@ -135,7 +138,7 @@ zfp_gb300_batch* zfp_gb300_batch_create(zfp_stream* const* streams, const zfp_fi
     return nullptr;
   }
   size_t offset_words = 0;
-  std::map<std::pair<int, int>, size_t> group_of;
+  std::map<std::tuple<int, int, bool>, size_t> group_of;   // (type, dims, reversible)
   for (size_t i = 0; i < count; i++) {
     zfp_stream* z = streams[i];
     const zfp_field* f = fields[i];
@@ -211,13 +214,15 @@ zfp_gb300_batch* zfp_gb300_batch_create(zfp_stream* const* streams, const zfp_fi
       }
     }
     b->jobs[i] = j;
-    const auto key = std::make_pair(fi.type, fi.dims);
+    const bool rev = z->minexp < ZFP_MIN_EXP;
+    const auto key = std::make_tuple(fi.type, fi.dims, rev);
     auto it = group_of.find(key);
     if (it == group_of.end()) {
       it = group_of.emplace(key, b->groups.size()).first;
       b->groups.emplace_back();
       b->groups.back().type = fi.type;
       b->groups.back().dims = fi.dims;
+      b->groups.back().lossy = !rev;
     }
     BatchGroup& g = b->groups[it->second];
     b->jobs[i].tile0 = g.total_tiles;
@@ -256,6 +261,7 @@ zfp_gb300_batch* zfp_gb300_batch_create(zfp_stream* const* streams, const zfp_fi
     LaunchArgs probe;
     std::memset(&probe, 0, sizeof probe);
     probe.jobs = g.d_jobs;
+    probe.multi_lossy = g.lossy;
     const uint32_t room = stage_room_any(g.type, g.dims, probe, b->direction == 0);
     g.img_words = std::min(g.tile_words, room);
   }

@@ -12,6 +12,7 @@ struct LaunchArgs {
   Job one;                // the job when njobs == 1
   const Job* jobs;        // device array when njobs > 1
   int njobs;
+  int multi_lossy;        // with `jobs`: no job of the array is reversible (the lossy-only kernels)
   LaunchScratch sc;
   uint32_t total_tiles;
   int use_ticket;

@@ -85,7 +85,11 @@ struct KernelTag {
 };
 
 // kernel variant: device job array -> multi-job kernel carrying both mode
-// paths; a single job -> the variant of its mode only.
+// paths, or the lossy path alone when no job of the array is reversible (the
+// reversible coder costs the lossy jobs registers: 186 for the 32-bit 3D
+// decoder, which the lossy one, held to four CTAs per SM like the
+// single-job kernels, does in 128); a single job -> the variant of its mode
+// only.
 // A 32-bit fixed-rate tile small enough for a fifth of an SM's shared memory
 // (with the bit planes) goes to the five-CTA kernels; so does a 32-bit
 // fixed-precision job whose largest tile fits there beside only its coded
@@ -143,7 +147,14 @@ static bool floor_encoder_fits(const Job& j) {
 
 template <typename S, int D, class F>
 static auto with_encoder(const LaunchArgs& a, F&& f) {
-  if (a.jobs) return f(KernelTag<encode_kernel<S, D, true, kAnyMode>>{});
+  if (a.jobs) {
+    if (a.multi_lossy) {
+      if constexpr (sizeof(S) == 4 && D == 3) return f(KernelTag<encode_kernel_occ<S, D, true, kLossyOnly, 4>>{});
+      else if constexpr (sizeof(S) == 8 && D == 3) return f(KernelTag<encode_kernel_occ<S, D, true, kLossyOnly, 3>>{});
+      else return f(KernelTag<encode_kernel<S, D, true, kLossyOnly>>{});
+    }
+    return f(KernelTag<encode_kernel<S, D, true, kAnyMode>>{});
+  }
   if (a.one.minexp < kMinExp) {
     if constexpr (sizeof(S) == 8 && D <= 3) return f(KernelTag<encode_kernel_occ<S, D, false, kRevOnly, 3>>{});
     else return f(KernelTag<encode_kernel<S, D, false, kRevOnly>>{});
@@ -160,7 +171,14 @@ static auto with_encoder(const LaunchArgs& a, F&& f) {
 
 template <typename S, int D, class F>
 static auto with_decoder(const LaunchArgs& a, F&& f) {
-  if (a.jobs) return f(KernelTag<decode_kernel<S, D, true, kAnyMode>>{});
+  if (a.jobs) {
+    if (a.multi_lossy) {
+      if constexpr (sizeof(S) == 4 && D == 3) return f(KernelTag<decode_kernel_occ<S, D, true, kLossyOnly, 4>>{});
+      else if constexpr (sizeof(S) == 8 && D == 3) return f(KernelTag<decode_kernel_occ<S, D, true, kLossyOnly, 3>>{});
+      else return f(KernelTag<decode_kernel<S, D, true, kLossyOnly>>{});
+    }
+    return f(KernelTag<decode_kernel<S, D, true, kAnyMode>>{});
+  }
   if (a.one.minexp < kMinExp) {
     if constexpr (sizeof(S) == 4 && D <= 3) return f(KernelTag<decode_kernel_occ<S, D, false, kRevOnly, 3>>{});
     else return f(KernelTag<decode_kernel<S, D, false, kRevOnly>>{});

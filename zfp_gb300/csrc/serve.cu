@@ -130,18 +130,19 @@ static void CUDART_CB lane_done(void* arg) {
 static cudaError_t launch_batch(Server* s, Lane* lane) {
   auto& reqs = lane->reqs;
   // group by (direction, type, dims) -- one launch each -- and assign tiles
-  std::map<std::tuple<int, int, int>, std::vector<size_t>> groups;
+  std::map<std::tuple<int, int, int, bool>, std::vector<size_t>> groups;
   for (size_t i = 0; i < reqs.size(); i++)
-    groups[{reqs[i]->direction, reqs[i]->fi.type, reqs[i]->fi.dims}].push_back(i);
+    groups[{reqs[i]->direction, reqs[i]->fi.type, reqs[i]->fi.dims, reqs[i]->z->minexp < ZFP_MIN_EXP}].push_back(i);
   // device layout: results | per group: jobs, scratch | block indexes
   size_t off = ((reqs.size() * sizeof(JobResult)) + 255) & ~(size_t)255;
-  struct G { int type, dims; std::vector<size_t> idx; uint32_t tiles = 0, img_words = 0; size_t jobs_off, scr_off,
-             scr_bytes; LaunchArgs one; };
+  struct G { int type, dims; bool lossy; std::vector<size_t> idx; uint32_t tiles = 0, img_words = 0; size_t jobs_off,
+             scr_off, scr_bytes; LaunchArgs one; };
   std::vector<G> gs;
   for (auto& kv : groups) {
     G g;
     g.type = std::get<1>(kv.first);
     g.dims = std::get<2>(kv.first);
+    g.lossy = !std::get<3>(kv.first);
     g.idx = kv.second;
     for (size_t i : g.idx) {
       Request& r = *reqs[i];
@@ -217,6 +218,7 @@ static cudaError_t launch_batch(Server* s, Lane* lane) {
       a.one = r0.job;
       a.jobs = (const Job*)(base + g.jobs_off);
       a.njobs = (int)g.idx.size();
+      a.multi_lossy = g.lossy;
     }
     const size_t t = (size_t)g.tiles + 1;
     char* p = base + g.scr_off;
