@@ -106,7 +106,7 @@ zfp_bool zfp_gb300_batch_get_tuning(const zfp_gb300_batch* batch, int* ctas_per_
  * requests of its class in arrival order while the bytes of all admitted,
  * unfinished requests (field span plus stream capacity) stay within
  * `hbm_budget`, and launches them as one batch (one persistent launch per
- * scalar type and dimensionality); a request completes with its batch, so
+ * scalar type, dimensionality and reversibility); a request completes with its batch, so
  * small requests never wait for large ones.  Requests that arrive while
  * batches run join the next batch on the next free lane of their class, so
  * work from different batches overlaps on the GPU.  Results are the same
