@@ -141,12 +141,12 @@ uint64_t decompress_t(const Geom& g, const zg::BlockParams& p, void* data, const
     uint64_t plane[P];
     for (int k = 0; k < P; k++) plane[k] = kPlaneJunk;
     // lossy blocks decode as the kLossyFloor kernels do (planes below P -
-    // maxprec untouched); 64-bit 3D blocks go through 32 slots regardless
+    // maxprec untouched); 64-bit 2D and 3D blocks go through 32 slots regardless
     if (p.minexp < zg::kMinExp) {
       zg::decode_block<S, D, zg::kRevOnly>(in, p, raw, zg::PlaneBuf{plane, 1});
     } else {
       zg::decode_block<S, D, zg::kLossyFloor>(in, p, raw, zg::PlaneBuf{plane, 1});
-      if (!(P == 64 && D == 3)) check_floor(plane, P, p.maxprec, P);
+      if (!(P == 64 && (D == 2 || D == 3))) check_floor(plane, P, p.maxprec, P);
     }
     size_t org[4], cnt[4];
     size_t bb = b;

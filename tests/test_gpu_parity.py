@@ -374,12 +374,12 @@ def test_pinned_stream_offsets(lib, oracle, cuda):
 
 def test_pinned_stream_uploaded_when_tiles_exceed_shared_memory(lib, oracle, cuda):
     """A page-locked stream whose decode tiles do not fit the decoder's shared
-    memory (2D 64-bit reversible noise: about 19 KB a tile beside 64 KB of
-    planes) is uploaded once instead of being read word by word across the
-    host link; 32-byte row stores write the 64-bit field.  Same bits as the
-    oracle either way."""
+    memory (4D 64-bit reversible noise: about 270 KB a tile of 128 blocks,
+    more than a CTA's shared memory) is uploaded once instead of being read
+    word by word across the host link; 32-byte row stores write the 64-bit
+    field.  Same bits as the oracle either way."""
     torch = cuda
-    shape = (200, 300)
+    shape = (16, 16, 16, 16)
     vals = np.random.default_rng(5).standard_normal(shape) * 1e3   # about 64 bits a value
     exp_words, _, prm = oracle_stream(oracle, vals, "reversible", None)
     nwords = len(exp_words) + 16

@@ -1151,10 +1151,10 @@ ZG_HD unsigned uncode_coeffs(Source& in, unsigned budget, unsigned maxprec,
   using U = typename std::make_unsigned<I>::type;
   constexpr int N = 1 << (2 * D);
   constexpr int P = 8 * sizeof(U);
-  if constexpr (P == 64 && N == 64) {
-    // 64-bit 3D blocks: the buffer holds 32 planes.  Planes 63-32 are
-    // decoded into it and their 32-bit halves transposed at once, then the
-    // same slots take planes 31-0.
+  if constexpr (P == 64 && (N == 64 || N == 16)) {
+    // 64-bit 2D and 3D blocks: the buffer holds 32 planes.  Planes 63-32
+    // are decoded into it and their 32-bit halves transposed at once, then
+    // the same slots take planes 31-0.
     const int kmin = (unsigned)P > maxprec ? P - (int)maxprec : 0;
     unsigned bits = budget, n = 0;
     int k = P - 1;

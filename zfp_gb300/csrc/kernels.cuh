@@ -685,11 +685,11 @@ ZG_HD constexpr unsigned plane_floor(bool multi, unsigned maxprec) {
   return multi ? 0u : kFloorKernel ? (maxprec < P ? P - maxprec : 0u) : half_planes<S, D>(maxprec) ? 32u : 0u;
 }
 
-// the decoder of 64-bit 3D blocks works through 32 planes at a time
+// the decoder of 64-bit 2D and 3D blocks works through 32 planes at a time
 // (uncode_coeffs), whatever the job
 template <typename S, int D>
 ZG_HD constexpr bool half_decode_planes() {
-  return sizeof(typename Traits<S>::UInt) == 8 && D == 3;
+  return sizeof(typename Traits<S>::UInt) == 8 && (D == 2 || D == 3);
 }
 
 template <typename S, int D, bool kEncode, bool kFloorKernel = false>
