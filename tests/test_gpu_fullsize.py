@@ -100,3 +100,44 @@ def test_config3_edge_shapes(lib, oracle, cuda):
     e = rng.integers(-(1 << 20), 1 << 20, size=(256, 256, 256), dtype=np.int32)
     out, _ = check_full(lib, oracle, torch, e, "reversible", None)
     assert np.array_equal(out, e)
+
+
+def test_field_beyond_32_bit_offsets(lib, oracle, cuda):
+    """A field of more than 2^32 values (float32 2048 x 2048 x 1040, 17 GB) at
+    fixed rate 1 (one 64-bit word per block): element offsets and stream bit
+    positions pass 32 bits.  Spot blocks -- the first, the last, and those
+    around the 2^32-th element -- must hold the oracle's code for their 64
+    values, and decompress to the oracle's decoding of it."""
+    torch = cuda
+    from tests.helpers import oracle_stream
+    nz, ny, nx = 1040, 2048, 2048
+    if torch.cuda.mem_get_info()[0] < 40 * 2**30:
+        pytest.skip("needs 40 GB of free device memory")
+    assert nz * ny * nx > 2**32
+    g = torch.Generator(device="cuda").manual_seed(9)
+    x = torch.randn((nz, ny, nx), dtype=torch.float32, device="cuda", generator=g)
+    nblocks = (nz // 4) * (ny // 4) * (nx // 4)
+    buf = torch.zeros(nblocks + 16, dtype=torch.int64, device="cuda")
+    n = (nx, ny, nz)
+    r, pos = zfp_run(lib, "compress", x.data_ptr(), capi.TYPE_FLOAT, n, (), "rate", 1, buf.data_ptr(), buf.numel() * 8)
+    assert r == nblocks * 8 and pos == nblocks * 64, lib.zfp_gb300_last_error()
+    out = torch.empty_like(x)
+    r2, _ = zfp_run(lib, "decompress", out.data_ptr(), capi.TYPE_FLOAT, n, (), "rate", 1, buf.data_ptr(),
+                    buf.numel() * 8)
+    assert r2 == r, lib.zfp_gb300_last_error()
+    nbx, nby = nx // 4, ny // 4
+    edge = 2**32 // (ny * nx) // 4          # the block row holding element 2^32
+    spots = [(0, 0, 0), (nbx - 1, nby - 1, nz // 4 - 1), (nbx - 1, nby - 1, edge - 1), (0, 0, edge),
+             (17, 301, edge), (nbx - 1, 0, edge + 1)]
+    for bx, by, bz in spots:
+        blk = x[4 * bz:4 * bz + 4, 4 * by:4 * by + 4, 4 * bx:4 * bx + 4].cpu().numpy()
+        exp, _, prm = oracle_stream(oracle, blk, "rate", 1)
+        b = bx + nbx * (by + nby * bz)
+        got = int(buf[b].item()) & (2**64 - 1)
+        assert got == int(exp[0]), (bx, by, bz)
+        ref = np.zeros_like(blk)
+        oracle.decompress(exp, ref, prm, 0)
+        dec = out[4 * bz:4 * bz + 4, 4 * by:4 * by + 4, 4 * bx:4 * bx + 4].cpu().numpy()
+        assert np.array_equal(dec.view(np.uint32), ref.view(np.uint32)), (bx, by, bz)
+    del x, out, buf
+    torch.cuda.empty_cache()
