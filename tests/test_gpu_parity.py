@@ -304,6 +304,19 @@ def test_errors_return_zero(lib, cuda):
     r, pos = zfp_run(lib, "compress", b.ctypes.data, 3, n, s, "reversible", None, buf.ctypes.data, 16 * 8)
     assert r == 0 and pos == 0
     assert "small" in lib.zfp_gb300_last_error().decode()
+    # the same for tiles too large for shared memory, written straight into a
+    # device stream: the blocks past its end are dropped and the call fails
+    torch = cuda
+    c = np.random.default_rng(8).standard_normal((40, 64, 90)) * 1e3
+    dc = torch.from_numpy(c).cuda()
+    dbuf = torch.zeros(1 << 16, dtype=torch.int64, device="cuda")
+    n3, s3 = geometry(c)
+    r, pos = zfp_run(lib, "compress", dc.data_ptr(), 4, n3, s3, "reversible", None, dbuf.data_ptr(), dbuf.numel() * 8)
+    assert r == 0 and pos == 0
+    assert "small" in lib.zfp_gb300_last_error().decode()
+    big = torch.zeros(1 << 21, dtype=torch.int64, device="cuda")   # and a buffer that holds it works
+    r, _ = zfp_run(lib, "compress", dc.data_ptr(), 4, n3, s3, "reversible", None, big.data_ptr(), big.numel() * 8)
+    assert r > 0, lib.zfp_gb300_last_error()
 
 
 def test_pinned_host_buffers_zero_copy(lib, oracle, cuda):
