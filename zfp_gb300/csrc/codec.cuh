@@ -72,7 +72,9 @@ struct BlockParams {
 // other path's registers out of the kernel.
 // kLossyFloor: lossy blocks whose planes below P - maxprec have no room in
 // the plane buffer (store_planes, decode_planes and uncode_coeffs skip them)
-enum ModeSel { kAnyMode = 0, kLossyOnly = 1, kRevOnly = 2, kLossyFloor = 3 };
+// kLossyHost: lossy blocks of an encode into host memory (kernels.cuh stages
+// its fixed-rate tiles, which the device-memory kernels do not)
+enum ModeSel { kAnyMode = 0, kLossyOnly = 1, kRevOnly = 2, kLossyFloor = 3, kLossyHost = 4 };
 
 template <int kSel>
 ZG_HD bool is_rev(const BlockParams& p) {
