@@ -249,49 +249,6 @@ struct SmemSink {
   }
 };
 
-// Sink of a fixed-rate block that starts and ends on a stream word: no
-// other block shares its words, so it writes them straight to the stream
-// (padding included: the stream is not zeroed beforehand).  `room` counts
-// the stream words from `out` on; stores past them are dropped and flagged.
-struct StreamSink {
-  uint64_t* out;
-  uint64_t room;
-  uint64_t word;
-  unsigned fill;
-  uint64_t acc;
-  unsigned* status;
-
-  __device__ __forceinline__ void store(uint64_t w) {
-    if (word < room) out[word] = w;
-    else atomicOr(status, (unsigned)kStatusOverflow);
-    word++;
-  }
-  // v must have no bits at or above n
-  __device__ __forceinline__ void put(uint64_t v, unsigned n) {
-    acc |= v << fill;
-    const unsigned t = fill + n;
-    if (t >= 64) {
-      store(acc);
-      acc = fill ? v >> (64 - fill) : 0;
-      fill = t - 64;
-    } else {
-      fill = t;
-    }
-  }
-  __device__ __forceinline__ void pad(unsigned n) {
-    unsigned t = fill + n;
-    while (t >= 64) {
-      store(acc);
-      acc = 0;
-      t -= 64;
-    }
-    fill = t;
-  }
-  __device__ __forceinline__ void finish() {
-    if (fill) store(acc);
-  }
-};
-
 // One block written straight into the stream from bit `fill` of word
 // `dst` on; the caller has checked that the block's words lie inside the
 // stream buffer.  Words the block covers whole are stored; its first word,
