@@ -74,7 +74,9 @@ struct BlockParams {
 // the plane buffer (store_planes, decode_planes and uncode_coeffs skip them)
 // kLossyHost: lossy blocks of an encode into host memory (kernels.cuh stages
 // its fixed-rate tiles, which the device-memory kernels do not)
-enum ModeSel { kAnyMode = 0, kLossyOnly = 1, kRevOnly = 2, kLossyFloor = 3, kLossyHost = 4 };
+// kFixedOnly: fixed-rate blocks only (the 64-bit 3D decoder: no block index
+// or variable-rate paths in the kernel)
+enum ModeSel { kAnyMode = 0, kLossyOnly = 1, kRevOnly = 2, kLossyFloor = 3, kLossyHost = 4, kFixedOnly = 5 };
 
 template <int kSel>
 ZG_HD bool is_rev(const BlockParams& p) {

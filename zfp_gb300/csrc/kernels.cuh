@@ -493,7 +493,7 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
   const bool active = b < job.nblocks;
   const uint64_t left = job.nblocks - (uint64_t)lt * kTile;
   const uint32_t nb = left < kTile ? (uint32_t)left : kTile;
-  const bool fixed = job.flags & kFixedRate;
+  const bool fixed = kSel == kFixedOnly || (job.flags & kFixedRate);
   const bool first = lt == 0, last = lt + 1 == job.ntiles;
   const BlockParams p{job.minbits, job.maxbits, job.maxprec, job.minexp};
   uint64_t* my_planes = planes + bi;   // plane k of this block at my_planes[k * kTile]
@@ -678,7 +678,7 @@ __device__ __forceinline__ void decode_tile(const Job& job, uint32_t gt, uint64_
   const uint64_t b0 = (uint64_t)lt * kTile;
   const uint64_t b = b0 + threadIdx.x;
   const bool active = b < job.nblocks;
-  const bool fixed = job.flags & kFixedRate;
+  const bool fixed = kSel == kFixedOnly || (job.flags & kFixedRate);
   const uint64_t nblk = job.nblocks - b0 < (uint64_t)kTile ? job.nblocks - b0 : (uint64_t)kTile;
 
   uint64_t Gs, Ge, start = 0, expect = 0;

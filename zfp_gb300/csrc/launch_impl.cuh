@@ -187,6 +187,9 @@ static auto with_decoder(const LaunchArgs& a, F&& f) {
     else return f(KernelTag<decode_kernel<S, D, false, kRevOnly>>{});
   }
   if constexpr (sizeof(S) == 8 && D <= 3) {
+    // fixed rate alone: without the block-index and stream-reading paths of
+    // variable rates the 3D decoder needs no spills (712 bytes otherwise), 2% faster
+    if (D == 3 && (a.one.flags & kFixedRate)) return f(KernelTag<decode_kernel_occ<S, D, false, kFixedOnly, 3>>{});
     return f(KernelTag<decode_kernel_occ<S, D, false, kLossyOnly, 3>>{});
   } else {
     if (five_ctas_floor<S, D>(a.one)) return f(KernelTag<decode_kernel_occ<S, D, false, kLossyFloor, 5>, true>{});
