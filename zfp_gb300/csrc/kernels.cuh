@@ -457,6 +457,12 @@ __device__ __forceinline__ void write_tile(const Job& job, const LaunchScratch& 
 // ---------------------------------------------------------------------------
 // encode one tile
 
+// Variable-rate tiles of more code than this are written straight into the
+// stream even where the image would hold them: their blocks, each tens of
+// words apart, store into the image with many bank conflicts, and the
+// look-back that direct writing waits for is spread over more work.
+constexpr uint32_t kStageMaxWords = 2048;
+
 // Bit planes first (with each block's length, for variable rates), then the
 // tile's place in the stream: its first bit G follows from the tile number
 // at a fixed rate, else from the decoupled look-back.
@@ -532,7 +538,7 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
   // path reachable for them cost the device-memory fp64 encoder 8% through
   // its register allocation
   const bool stage = !fixed || kSel == kLossyHost;
-  if (kStagedOnly || (stage && total && need <= img_cap(img_words))) {
+  if (kStagedOnly || (stage && total && need <= img_cap(img_words) && need <= kStageMaxWords)) {
     const uint32_t nw = kStagedOnly ? min(need, img_cap(img_words)) : need;   // stores past it are flagged
     for (uint32_t i = bi; i < nw; i += kTile) img[img_phys(i)] = 0;
     __syncthreads();
