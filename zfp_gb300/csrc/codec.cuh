@@ -72,15 +72,16 @@ struct BlockParams {
 // other path's registers out of the kernel.
 // kLossyFloor: lossy blocks whose planes below P - maxprec have no room in
 // the plane buffer (store_planes, decode_planes and uncode_coeffs skip them)
-// kLossyHost: lossy blocks of an encode into host memory (kernels.cuh stages
-// its fixed-rate tiles, which the device-memory kernels do not)
+// kLossyHost / kRevHost: lossy / reversible blocks of an encode into host
+// memory (kernels.cuh stages every tile the image holds, which the
+// device-memory kernels do not do for fixed-rate or large tiles)
 // kFixedOnly: fixed-rate blocks only (the 64-bit 3D decoder: no block index
 // or variable-rate paths in the kernel)
-enum ModeSel { kAnyMode = 0, kLossyOnly = 1, kRevOnly = 2, kLossyFloor = 3, kLossyHost = 4, kFixedOnly = 5 };
+enum ModeSel { kAnyMode = 0, kLossyOnly = 1, kRevOnly = 2, kLossyFloor = 3, kLossyHost = 4, kFixedOnly = 5, kRevHost = 6 };
 
 template <int kSel>
 ZG_HD bool is_rev(const BlockParams& p) {
-  return kSel == kRevOnly || (kSel == kAnyMode && p.minexp < kMinExp);
+  return kSel == kRevOnly || kSel == kRevHost || (kSel == kAnyMode && p.minexp < kMinExp);
 }
 
 // ---------------------------------------------------------------------------

@@ -20,7 +20,7 @@ enum JobFlags : uint32_t {
   kVec32 = 16u,      // with kVecOk, 64-bit rows (32 bytes) are 32-byte aligned: one access per row
   kStreamHost = 32u, // encode: the stream is host memory written in place over the host link, where
                      // only whole coalesced lines go at speed: tiles are staged in shared memory
-                     // whenever they fit (fixed-rate ones by the kLossyHost kernels)
+                     // whenever they fit (by the kLossyHost / kRevHost kernels)
 };
 
 enum JobStatus : uint32_t {

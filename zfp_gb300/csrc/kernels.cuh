@@ -534,11 +534,13 @@ __device__ __forceinline__ void encode_tile(const Job& job, const LaunchScratch&
   // largest possible tile (see with_encoder), so it is built with this path
   // alone: measured 6% faster at precision 20 than with both paths.
   constexpr bool kStagedOnly = kSel == kLossyFloor;
-  // fixed-rate tiles are staged only by the host-stream kernel: making the
-  // path reachable for them cost the device-memory fp64 encoder 8% through
-  // its register allocation
-  const bool stage = !fixed || kSel == kLossyHost;
-  if (kStagedOnly || (stage && total && need <= img_cap(img_words) && need <= kStageMaxWords)) {
+  // fixed-rate and large tiles are staged only by the host-stream kernels,
+  // whose stream is written across the host link: making the path
+  // reachable for fixed-rate tiles cost the device-memory fp64 encoder 8%
+  // through its register allocation
+  constexpr bool kHost = kSel == kLossyHost || kSel == kRevHost;
+  const bool stage = !fixed || kHost;
+  if (kStagedOnly || (stage && total && need <= img_cap(img_words) && (kHost || need <= kStageMaxWords))) {
     const uint32_t nw = kStagedOnly ? min(need, img_cap(img_words)) : need;   // stores past it are flagged
     for (uint32_t i = bi; i < nw; i += kTile) img[img_phys(i)] = 0;
     __syncthreads();

@@ -147,9 +147,11 @@ static bool floor_encoder_fits(const Job& j) {
 
 template <typename S, int D, class F>
 static auto with_encoder(const LaunchArgs& a, F&& f) {
-  // a fixed-rate encode into host memory stages its tiles (kStreamHost)
-  if (!a.jobs && (a.one.flags & kStreamHost) && (a.one.flags & kFixedRate))
+  // an encode into host memory stages its tiles (kStreamHost)
+  if (!a.jobs && (a.one.flags & kStreamHost)) {
+    if (a.one.minexp < kMinExp) return f(KernelTag<encode_kernel<S, D, false, kRevHost>>{});
     return f(KernelTag<encode_kernel<S, D, false, kLossyHost>>{});
+  }
   if (a.jobs) {
     if (a.multi_lossy) {
       if constexpr (sizeof(S) == 4 && D == 3) return f(KernelTag<encode_kernel_occ<S, D, true, kLossyOnly, 4>>{});
