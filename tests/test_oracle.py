@@ -125,3 +125,37 @@ def test_oracle_matches_reference_random(oracle, ref):
                     assert np.array_equal(out.view(np.uint8), np.ascontiguousarray(ref_out).view(np.uint8))
                     n += 1
     assert n > 250
+
+
+def test_oracle_matches_reference_tiny_budgets(oracle, ref):
+    """Expert budgets of a few bits per block, as the GPU tests use them: the
+    oracle must write and read what the reference does, including integer
+    blocks of no bits (maxbits 0) and float budgets below the block header,
+    where the reference's remaining budget wraps around and its blocks are
+    coded in full (the stream then runs past zfp_stream_maximum_size, so the
+    buffers here are sized for full blocks)."""
+    rng = np.random.default_rng(78)
+    params = [(0, 0, 64, -1074), (0, 1, 64, -1074), (1, 1, 64, -1074), (0, 3, 1, -1074), (2, 2, 64, -1074),
+              (0, 9, 64, -1074), (12, 12, 64, -1074), (0, 20, 3, 0)]
+    n = 0
+    for dims in (1, 2, 3, 4):
+        for dtype in (np.float32, np.float64, np.int32, np.int64):
+            for prm_arg in params:
+                if np.dtype(dtype).kind == "f" and prm_arg[1] < 1:
+                    continue   # a float block codes at least one bit
+                shape = tuple(int(v) for v in rng.integers(1, {1: 40, 2: 12, 3: 7, 4: 5}[dims], size=dims))
+                if np.dtype(dtype).kind == "f":
+                    a = (np.cumsum(rng.standard_normal(shape), axis=-1) * 10.0 ** rng.uniform(-3, 3)).astype(dtype)
+                else:
+                    a = rng.integers(-(1 << 20), 1 << 20, size=shape).astype(dtype)
+                expect, ref_out, prm = _ref_roundtrip(ref, a, "expert", prm_arg)
+                blocks = int(np.prod([(v + 3) // 4 for v in shape]))
+                room = blocks * (4 ** dims * 65 + 64) // 64 + 16
+                words, end = oracle.compress(a, prm, words=np.zeros(room, dtype=np.uint64))
+                nw = (end + 63) // 64
+                assert nw == len(expect) and np.array_equal(words[:nw], expect), (dims, dtype, prm_arg, shape)
+                out = np.zeros(a.shape, dtype=a.dtype)
+                oracle.decompress(expect, out, prm)
+                assert np.array_equal(out.view(np.uint8), ref_out.view(np.uint8)), (dims, dtype, prm_arg, shape)
+                n += 1
+    assert n >= 100
