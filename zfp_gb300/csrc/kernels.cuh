@@ -468,13 +468,15 @@ constexpr uint32_t kStageMaxWords = 2048;
 // at a fixed rate, else from the decoupled look-back.
 //
 // A variable-rate tile whose code fits the shared-memory image (`img`,
-// `img_words` words) is coded there while the look-back runs, and copied
-// out at G by write_tile: the look-back's wait for the tiles before it
-// overlaps the coding.
+// `img_words` words) and kStageMaxWords is coded there while the look-back
+// runs, and copied out at G by write_tile: the look-back's wait for the
+// tiles before it overlaps the coding.  The host-stream kernels stage every
+// tile the image holds, fixed-rate and large ones included, so that only
+// whole lines cross the host link.
 //
 // Every other tile -- fixed-rate ones, whose G needs no look-back, and
-// variable-rate ones too large for the image -- is coded straight into the
-// stream (SeamSink).  Boundary i of the tile (block i's first bit; boundary
+// variable-rate ones too large for the image or the cap -- is coded
+// straight into the stream (SeamSink).  Boundary i of the tile (block i's first bit; boundary
 // nb is the tile's end) lies in stream word W_i; a word holding a boundary
 // inside it is shared, and its seam entry is that of the first boundary in
 // the word.  Blocks of 64 bits or more put every boundary in a word of its
