@@ -62,3 +62,24 @@ def test_single_rank_is_local_time():
     import bench
     assert bench.job_ms(12.5, 1, "cpu") == 12.5
     assert bench.job_gbs(2 * 10**9, 5, 1, 1000.0) == pytest.approx(10.0)
+
+
+def test_reference_arm_prints_the_bench_line():
+    """`bench.py --impl reference` runs the reference's own CPU codec (its
+    library compiled from its sources, else the oracle port) with no GPU and
+    prints one JSON line of the bench contract, tagged as the reference."""
+    import json
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--small", "--steps", "1",
+                        "--warmup", "1"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, r.stdout[-2000:]
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "GB/s" and d["value"] > 0 and d["higher_is_better"] is True
+    for key in ("metric", "n_gpus", "steps", "warmup", "ms_per_step", "scaling", "dtype", "data", "config"):
+        assert key in d, key
+    cb = d["cpu_baseline"]
+    assert cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
